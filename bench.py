@@ -1,0 +1,383 @@
+#!/usr/bin/env python3
+"""Benchmark of the Giant-Impact hot path on GB300.
+
+Workload (default): the plain two-body impact -- a 60,000-body target and a
+6,000-body impactor (30 % Fe core each), seeded, settled on the GPU with the
+damped separate-body step, spun about z at 0.5 of breakup, impactor at 45
+degrees and 1.2 x the mutual escape speed, 66,000 bodies in total, FP32,
+dt = 1e-3.  A step is one fused force + kick-drift pass over all 66,000
+bodies: N (N - 1) = 4.356e9 pair interactions.
+
+Timing: W untimed warm-up steps, then K steps each bracketed by CUDA events
+on the launching stream; L2 (129 MB) is flushed by writing a 256 MB buffer
+between timed steps (outside the events).  value = interactions / s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's force / move loop restated on the
+host (the oracle's reference-exact FP32 port, OpenMP over all host cores) on
+the same workload, one bounded i-sample per step.  Multi-GPU (torchrun):
+independent replicas, one impact per GPU, value = sum over GPUs.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "giant-impact_gb300")
+sys.path.insert(0, PKG)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+FLOP_PER_INTERACTION = 20  # conventional N-body count (SURVEY: sub 3, r2 3, rsqrt, scale 4, FMA 3x2)
+N_TARGET, N_IMPACTOR = 60000, 6000
+
+
+def _load(name, path):
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, path)
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def args_parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--settle-steps", type=int, default=1500)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ref-gpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+def dist_setup(backend):
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend)
+    return rank, local, world
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(gi, torch, wl, seed, settle_steps):
+    pos, vel, nfe = wl.impact(gi, torch, N_TARGET, N_IMPACTOR, seed=seed, settle_steps=settle_steps)
+    return pos, vel, nfe
+
+
+def cpu_baseline(orc, pos, vel, nfe, p, seconds):
+    """Reference-exact FP32 force loop (oracle port, OpenMP, all host cores)
+    on a bounded sample of i-bodies against all N j-bodies."""
+    import numpy as np
+    n = len(pos)
+    run = [(0, n, nfe, 0, 0.0, 0.0, 0.0, 0.0)]
+    rng = np.random.default_rng(0)
+    k = 64
+    while True:
+        idx = np.sort(rng.choice(n, min(k, n), replace=False)).astype(np.int32)
+        t0 = time.perf_counter()
+        orc.forces_ref_subset(pos, vel, idx, run, p)
+        dt = time.perf_counter() - t0
+        if dt >= seconds or k >= n:
+            break
+        k = min(n, max(2 * k, int(k * seconds / max(dt, 1e-3) * 1.05)))
+    inter = len(idx) * (n - 1)
+    return {"value": inter / dt, "unit": "interactions/s", "cores": orc.max_threads(),
+            "kind": "port",
+            "sample": f"{len(idx)} seeded i-bodies x all {n} j-bodies of the 66,000-body impact "
+                      f"state ({inter:.3e} interactions, {dt:.1f} s), reference-exact FP32 force loop"}
+
+
+def ref_gpu_baseline(gi, orc, torch, pos, vel, nfe, p, steps=6):
+    """The reference's own kernels (getForcesCollisionSingleGPU +
+    moveBodiesCollisionSingleGPU, cut from its sources, -O3 sm_103a) on the
+    same state padded to a multiple of 256 with distant Si bodies."""
+    import ctypes as C
+    import numpy as np
+    ref = orc.ref_lib()
+    if ref is None:
+        return None
+    n = len(pos)
+    nr = ((n + 255) // 256) * 256
+    pp = np.zeros((nr, 4), np.float32)
+    vv = np.zeros((nr, 4), np.float32)
+    pp[:n], vv[:n] = pos, vel
+    pp[n:, :3] = 1e6 + np.arange(nr - n)[:, None] * 10.0
+    vv[n:, 3] = p.MassSi
+    # reference normalisation m_Si = 1 (the kernel hard-codes it)
+    mu = p.MassSi
+    rp = gi.params_from_material(1.0, 1.0, p.MassFe / mu, 1.0, 5.0 / mu**2, 1.5 / mu**2, 0.02,
+                                 0.01, 0.002, 0.001)
+    fc = gi.collision_consts(rp, nfe)
+    dt = 1e-3 * mu ** 0.5
+    mc = gi.MoveCollisionConsts(dt, dt / rp.MassFe, dt / rp.MassSi, nfe)
+    dp = torch.from_numpy(pp).cuda()
+    dv = torch.from_numpy(vv / np.float32([mu ** 0.5, mu ** 0.5, mu ** 0.5, 1.0])).cuda()
+    df = torch.zeros_like(dp)
+    s = torch.cuda.current_stream().cuda_stream
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    for k in range(steps + 2):
+        if k == 2:
+            torch.cuda.synchronize()
+            ev[0].record()
+        assert ref.giref_forces_collision(dp.data_ptr(), dv.data_ptr(), df.data_ptr(), C.byref(fc),
+                                          nr, s) == 0
+        assert ref.giref_move_collision(dp.data_ptr(), dv.data_ptr(), df.data_ptr(), C.byref(mc),
+                                        nr, s) == 0
+    ev[1].record()
+    torch.cuda.synchronize()
+    ms = ev[0].elapsed_time(ev[1]) / steps
+    inter = nr * (nr - 1)
+    return {"value": inter / (ms * 1e-3), "unit": "interactions/s", "ms_per_step": ms,
+            "n": nr, "what": "reference getForcesCollisionSingleGPU + moveBodiesCollisionSingleGPU, "
+                             "-O3 sm_103a, same GB300, state padded to N % 256 == 0"}
+
+
+def run_ours(a):
+    import numpy as np
+    import torch
+    rank, local, world = dist_setup("nccl")
+    torch.cuda.set_device(local)
+    b = _load("gi_build", os.path.join(PKG, "gi_build.py"))
+    if not os.path.exists(os.path.join(PKG, "lib", "libgi.so")):
+        b.build_all()
+    gi = _load("gi", os.path.join(PKG, "gi.py"))
+    wl = _load("gi_workloads", os.path.join(PKG, "gi_workloads.py"))
+    import oracle as orc
+
+    ctx = gi.Context(local)
+    pos, vel, nfe = make_workload(gi, torch, wl, 2 + rank, a.settle_steps)
+    n = len(pos)
+    p = wl.params(gi)
+    run = wl.run_desc(gi, 0, n, nfe)
+    dp = torch.from_numpy(pos).cuda()
+    dv = torch.from_numpy(vel).cuda()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    for _ in range(max(3, a.warmup)):
+        ctx.step(dp.data_ptr(), dv.data_ptr(), [run], p, 1, s)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(a.steps)]
+    t_wall = time.perf_counter()
+    for k in range(a.steps):
+        flush.fill_(float(k))
+        evs[k][0].record(stream)
+        ctx.step(dp.data_ptr(), dv.data_ptr(), [run], p, 1, s)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms = total_ms / a.steps
+    inter = n * (n - 1)
+    value = world * inter * a.steps / (total_ms * 1e-3)
+    state_ok = bool(torch.isfinite(dp).all().item() and torch.isfinite(dv).all().item())
+
+    # end-to-end through the host-buffer entry point (pinned memory, copies timed)
+    hp = torch.from_numpy(dp.cpu().numpy()).pin_memory()
+    hv = torch.from_numpy(dv.cpu().numpy()).pin_memory()
+    k_e2e = max(3, min(a.steps, 20))
+    ctx.run_host(hp.data_ptr(), hv.data_ptr(), n, [run], p, 1, s)
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        ctx.run_host(hp.data_ptr(), hv.data_ptr(), n, [run], p, 1, s)
+    e2e_s = (time.perf_counter() - t0) / k_e2e
+    e2e = {"value": world * inter / e2e_s, "unit": "interactions/s",
+           "h2d_bytes_per_step": 2 * n * 16, "d2h_bytes_per_step": 2 * n * 16,
+           "api": "gi_run_host (host pos/vel in, 1 fused step, host pos/vel out, synchronous)"}
+
+    result = None
+    if rank == 0:
+        peak = gi.measure_ffma_peak(local)
+        info = gi.device_info(local)
+        achieved = inter * FLOP_PER_INTERACTION / (ms * 1e-3) / 1e12
+        ipt, jchunk = ctx.get_tuning(n)
+        roof = {"bound": "fp32_ffma", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_source": "measured FFMA microbenchmark (gi_measure_ffma_peak) on this GPU "
+                               "in this run; MEASURED_PEAKS.json has no FP32 figure",
+                "nominal_peak": info["sm_count"] * 128 * 2 * 2.07e9 / 1e12,
+                "kernel": f"gi::force_kernel<{ipt},KAHAN,STEP> (fused force + kick-drift)",
+                "flop_per_interaction": FLOP_PER_INTERACTION,
+                "interactions_per_launch": inter}
+        cpu = None
+        if not a.no_cpu_baseline:
+            cpu = cpu_baseline(orc, dp.cpu().numpy(), dv.cpu().numpy(), nfe, p, a.cpu_seconds)
+        refgpu = None
+        if not a.no_ref_gpu:
+            refgpu = ref_gpu_baseline(gi, orc, torch, pos, vel, nfe, p)
+        result = {
+            "metric": "interactions/s", "value": value, "unit": "interactions/s", "n_gpus": world,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded, settled on the GPU)",
+            "config": {"workload": "plain two-body impact: 60,000-body target + 6,000-body impactor, "
+                                   "30% Fe, spin 0.5 breakup, 45 deg, 1.2 v_esc, dt 1e-3",
+                       "n_bodies": n, "interactions_per_step": inter,
+                       "accumulation": "kahan (FP32 tiles of 128, compensated across tiles)",
+                       "tuning": {"i_per_thread": ipt, "jchunk": jchunk},
+                       "l2": "flushed between timed steps (256 MB write, outside the events)",
+                       "parallelism": f"replicas x{world}"},
+            "fp32_tflops": achieved, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "ref_gpu": refgpu, "clocks": clk, "gpu_launches": a.steps,
+            "wall_s_timed_region": t_wall, "state_finite": state_ok,
+            "step_ms_min_max": [min(step_ms), max(step_ms)],
+        }
+        print(json.dumps(result))
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return result
+
+
+def run_reference(a):
+    """Reference arm: the reference's force/move loop on the host cores."""
+    import numpy as np
+    rank, local, world = dist_setup("gloo")
+    if rank != 0:
+        return None
+    import oracle as orc
+    gi = _load("gi", os.path.join(PKG, "gi.py"))
+    wl = _load("gi_workloads", os.path.join(PKG, "gi_workloads.py"))
+    b = _load("gi_build", os.path.join(PKG, "gi_build.py"))
+    b.build_oracle()
+    p = wl.params(gi)
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("no GPU for input preparation")
+        pos, vel, nfe = make_workload(gi, torch, wl, 2, a.settle_steps)
+        prep = "state prepared (settled) on the GPU, then copied to the host"
+    except Exception as e:  # input preparation only; the timed loop is pure host code
+        pt, vt, fet = wl.raw_body(gi, 2, N_TARGET, 0.0, 1.0)
+        pi, vi, fei = wl.raw_body(gi, 1002, N_IMPACTOR, 2.0, 3.0)
+        pos, vel, nfe = wl.spin_and_place(np.concatenate([pt, pi]), np.concatenate([vt, vi]),
+                                          N_TARGET, N_IMPACTOR, fet, fei)
+        prep = f"unsettled bodies ({e})"
+    n = len(pos)
+    run = [(0, n, nfe, 0, wl.DT, wl.DT / 1.0, wl.DT / 0.4, 0.0)]
+    rng = np.random.default_rng(1)
+    # size one step's i-sample so that warm-up + steps stay within ~3 minutes
+    k = 256
+    idx = np.sort(rng.choice(n, k, replace=False)).astype(np.int32)
+    t0 = time.perf_counter()
+    orc.forces_ref_subset(pos, vel, idx, run, p)
+    t1 = time.perf_counter() - t0
+    per_step_budget = 150.0 / max(1, a.steps + a.warmup)
+    k = int(max(64, min(n, k * per_step_budget / max(t1, 1e-4))))
+    times = []
+    for s in range(a.warmup + a.steps):
+        idx = np.sort(rng.choice(n, k, replace=False)).astype(np.int32)
+        t0 = time.perf_counter()
+        orc.forces_ref_subset(pos, vel, idx, run, p)
+        dt = time.perf_counter() - t0
+        if s >= a.warmup:
+            times.append(dt)
+    inter = k * (n - 1)
+    value = inter * len(times) / sum(times)
+    full_step_ms = n * (n - 1) / value * 1e3
+    line = {"impl": "reference", "metric": "interactions/s", "value": value, "unit": "interactions/s",
+            "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": full_step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "plain two-body impact: 60,000 + 6,000 bodies (66,000)",
+                       "n_bodies": n, "input": prep},
+            "cpu_baseline": {"value": value, "unit": "interactions/s", "cores": orc.max_threads(),
+                             "kind": "port",
+                             "sample": f"per step {k} seeded i-bodies x all {n} j-bodies "
+                                       f"({inter:.3e} interactions); reference-exact FP32 restatement "
+                                       f"of getForcesCollisionSingleGPU (the reference has no CPU "
+                                       f"implementation of this path)"},
+            "e2e": {"value": value, "unit": "interactions/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return line
+
+
+if __name__ == "__main__":
+    args = args_parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)

@@ -1,0 +1,271 @@
+// gi_aux.cu -- the memory-bound kernels around the force pass: kick-drift,
+// FP64 diagnostic reductions, the pair potential, and the FFMA throughput
+// microbenchmark that gives the force kernel its roofline denominator.
+#include "gi_internal.h"
+
+namespace gi {
+
+// v += (F - damp v) dt/m ; x += v dt, w carried through.
+// Reference: moveBodiesCollisionSingleGPU (Code/ImpactCode/impactAddTime.cu:
+// 379-394) and moveBodiesDampedSeperate (Code/GenerateTargetImpactorCode/
+// generateTargetImpactor.cu:628-664).  80 B per body (read pos, vel, force;
+// write pos, vel).
+__global__ void __launch_bounds__(256)
+move_kernel(float4 *__restrict__ pos, float4 *__restrict__ vel,
+            const float4 *__restrict__ force, const __grid_constant__ LaunchTable tab)
+{
+    const RunDev &R = tab.runs[blockIdx.y];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= R.n) return;
+    const int i = R.offset + k;
+    const float dtm = (k < R.nfe) ? R.dtm_fe : R.dtm_si;
+    const float4 f = __ldg(&force[i]);
+    float4 v = vel[i];
+    float4 p = pos[i];
+    v.x = __fmaf_rn(__fmaf_rn(-R.damp, v.x, f.x), dtm, v.x);
+    v.y = __fmaf_rn(__fmaf_rn(-R.damp, v.y, f.y), dtm, v.y);
+    v.z = __fmaf_rn(__fmaf_rn(-R.damp, v.z, f.z), dtm, v.z);
+    p.x = __fmaf_rn(v.x, R.dt, p.x);
+    p.y = __fmaf_rn(v.y, R.dt, p.y);
+    p.z = __fmaf_rn(v.z, R.dt, p.z);
+    vel[i] = v;
+    pos[i] = p;
+}
+
+// ----------------------------------------------------------------- diag --
+
+__device__ __forceinline__ bool in_scope(const unsigned char *label, int i, int scope)
+{
+    if (label == nullptr || scope == 0) return true;
+    const unsigned char l = label[i];
+    if (scope == 1) return l == 1 || l == 2;
+    if (scope == 2) return l == 1;
+    return l == 2;
+}
+
+template <int NV>
+__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *dst)
+{
+    __shared__ double sh[NV][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        double x = v[c];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[c][warp] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double x = 0.0;
+        const int nw = blockDim.x >> 5;
+        for (int w = 0; w < nw; ++w) x += sh[threadIdx.x][w];
+        dst[threadIdx.x] = x;
+    }
+}
+
+// Pass 1: mass, sum m x, sum m v, kinetic energy, count (9 doubles / block).
+__global__ void __launch_bounds__(256)
+diag_pass1(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+           const unsigned char *__restrict__ label, int scope, int off, int n,
+           int nfe, double mfe, double msi, double *__restrict__ work)
+{
+    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = off + k;
+        if (!in_scope(label, i, scope)) continue;
+        const double m = (k < nfe) ? mfe : msi;
+        const float4 p = pos[i], u = vel[i];
+        v[0] += m;
+        v[1] += m * p.x; v[2] += m * p.y; v[3] += m * p.z;
+        v[4] += m * u.x; v[5] += m * u.y; v[6] += m * u.z;
+        v[7] += 0.5 * m * ((double)u.x * u.x + (double)u.y * u.y + (double)u.z * u.z);
+        v[8] += 1.0;
+    }
+    block_reduce_store<9>(v, work + 16 * blockIdx.x);
+}
+
+// Finalise pass 1 in block order; out = [mass, com3, vcom3, -, -, -, ke, p3, count].
+__global__ void diag_fin1(const double *__restrict__ work, int nblocks, double *out)
+{
+    if (threadIdx.x != 0) return;
+    double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int b = 0; b < nblocks; ++b)
+        for (int c = 0; c < 9; ++c) t[c] += work[16 * b + c];
+    const double m = t[0];
+    out[0] = m;
+    for (int c = 0; c < 3; ++c) {
+        out[1 + c] = m > 0.0 ? t[1 + c] / m : 0.0;
+        out[4 + c] = m > 0.0 ? t[4 + c] / m : 0.0;
+        out[11 + c] = t[4 + c];
+    }
+    out[10] = t[7];
+    out[14] = t[8];
+}
+
+// Pass 2: angular momentum about the com, relative to the com velocity
+// (impactBasicFunctions.h:507-652 in double).
+__global__ void __launch_bounds__(256)
+diag_pass2(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+           const unsigned char *__restrict__ label, int scope, int off, int n,
+           int nfe, double mfe, double msi, const double *__restrict__ out,
+           double *__restrict__ work)
+{
+    const double cx = out[1], cy = out[2], cz = out[3];
+    const double ux = out[4], uy = out[5], uz = out[6];
+    double v[3] = {0, 0, 0};
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = off + k;
+        if (!in_scope(label, i, scope)) continue;
+        const double m = (k < nfe) ? mfe : msi;
+        const float4 p = pos[i], u = vel[i];
+        const double rx = p.x - cx, ry = p.y - cy, rz = p.z - cz;
+        const double wx = u.x - ux, wy = u.y - uy, wz = u.z - uz;
+        v[0] += (ry * wz - rz * wy) * m;
+        v[1] += -(rx * wz - rz * wx) * m;
+        v[2] += (rx * wy - ry * wx) * m;
+    }
+    block_reduce_store<3>(v, work + 16 * blockIdx.x);
+}
+
+__global__ void diag_fin2(const double *__restrict__ work, int nblocks, double *out)
+{
+    if (threadIdx.x != 0) return;
+    double t[3] = {0, 0, 0};
+    for (int b = 0; b < nblocks; ++b)
+        for (int c = 0; c < 3; ++c) t[c] += work[16 * b + c];
+    out[7] = t[0]; out[8] = t[1]; out[9] = t[2];
+}
+
+// -------------------------------------------------------------- potential --
+// Per i-block of 128 bodies, sum over every j of the run of U(r_ij):
+// far pairs -gm_i gm_j / r (FP32, rsqrt refined by one Newton step), contact
+// pairs the full-K polynomial; 128-term tiles folded in FP64.  One double
+// per block (already halved), summed by the host in block order.
+__global__ void __launch_bounds__(GI_NT)
+potential_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
+                 double *__restrict__ per_block)
+{
+    __shared__ float4 sP[GI_NT];
+    __shared__ double sRed[GI_NT / 32];
+    const int tid = threadIdx.x;
+    // Locate the run: runs[r].item_start is the first block of run r.
+    int lo = 0, hi = tab.nruns - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (tab.runs[mid].item_start <= (int)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+    }
+    const RunDev &R = tab.runs[lo];
+    const PairDev &P = tab.params[R.param];
+    const int rbeg = R.offset, rend = R.offset + R.n, sw = R.offset + R.nfe;
+    const int i = rbeg + (blockIdx.x - R.item_start) * GI_NT + tid;
+    const bool valid = i < rend;
+    float xi = GI_FAR_I, yi = GI_FAR_I, zi = GI_FAR_I;
+    if (valid) { const float4 p = pos[i]; xi = p.x; yi = p.y; zi = p.z; }
+    const bool ife = i < sw;
+    double acc = 0.0;
+    for (int jt = rbeg; jt < rend; jt += GI_NT) {
+        const int j = jt + tid;
+        float4 pj;
+        if (j < rend) { pj = pos[j]; pj.w = (j < sw) ? P.gm_fe : P.gm_si; }
+        else pj = make_float4(GI_FAR_J, GI_FAR_J, GI_FAR_J, 0.0f);
+        __syncthreads();
+        sP[tid] = pj;
+        __syncthreads();
+        float far = 0.0f, near = 0.0f;
+#pragma unroll 4
+        for (int jj = 0; jj < GI_NT; ++jj) {
+            const float4 q = sP[jj];
+            const float dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
+            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            const bool c = r2 < 1.0f;
+            // Contact pairs (and the self pair, r2 == 0) are taken out of the
+            // far sum; rr keeps rsqrt finite for them.
+            const float rr = c ? 1.0f : r2;
+            float ri = rsqrtf(rr);
+            ri = ri * __fmaf_rn(-0.5f * rr, ri * ri, 1.5f);  // one Newton-Raphson step
+            far = __fmaf_rn(c ? 0.0f : q.w, ri, far);
+            if (c && (jt + jj) != i && valid) {
+                const int test = ife + ((jt + jj) < sw);
+                const float G = P.G[test], K = P.K[test];
+                const float r = __fsqrt_rn(r2);
+                const float u = -G + G * (r - 1.0f) - K * (r - r * r * r * (1.0f / 3.0f) - 2.0f / 3.0f);
+                near += u;
+            }
+        }
+        const float gmi = ife ? P.gm_fe : P.gm_si;
+        acc += -(double)gmi * (double)far + (double)near;
+    }
+    if (!valid) acc = 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((tid & 31) == 0) sRed[tid >> 5] = acc;
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0.0;
+        for (int w = 0; w < GI_NT / 32; ++w) t += sRed[w];
+        per_block[blockIdx.x] = 0.5 * t;
+    }
+}
+
+// ------------------------------------------------------------ FFMA peak --
+// Eight independent FMA chains per thread; 2 flops per FMA.
+__global__ void __launch_bounds__(256) ffma_peak_kernel(float *sink, int iters)
+{
+    float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1e-7f, a2 = a0 + 2e-7f, a3 = a0 + 3e-7f;
+    float a4 = a0 + 4e-7f, a5 = a0 + 5e-7f, a6 = a0 + 6e-7f, a7 = a0 + 7e-7f;
+    const float m = 0.9999999f, c = 1e-7f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+            a0 = __fmaf_rn(a0, m, c); a1 = __fmaf_rn(a1, m, c);
+            a2 = __fmaf_rn(a2, m, c); a3 = __fmaf_rn(a3, m, c);
+            a4 = __fmaf_rn(a4, m, c); a5 = __fmaf_rn(a5, m, c);
+            a6 = __fmaf_rn(a6, m, c); a7 = __fmaf_rn(a7, m, c);
+        }
+    }
+    const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == 1234.5f) sink[blockIdx.x] = s;
+}
+
+}  // namespace gi
+
+cudaError_t gi_launch_move(float4 *pos, float4 *vel, const float4 *force,
+                           const LaunchTable &tab, cudaStream_t s)
+{
+    int maxn = 0;
+    for (int r = 0; r < tab.nruns; ++r) maxn = tab.runs[r].n > maxn ? tab.runs[r].n : maxn;
+    if (maxn == 0 || tab.nruns == 0) return cudaSuccess;
+    dim3 grid((maxn + 255) / 256, tab.nruns), block(256);
+    gi::move_kernel<<<grid, block, 0, s>>>(pos, vel, force, tab);
+    return cudaGetLastError();
+}
+
+cudaError_t gi_launch_diag(const float4 *pos, const float4 *vel,
+                           const unsigned char *label, int scope,
+                           const RunDev &run, const PairDev &par, float mass_fe,
+                           float mass_si, double *work, int nblocks, double *out_dev,
+                           cudaStream_t s)
+{
+    (void)par;
+    gi::diag_pass1<<<nblocks, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n,
+                                           run.nfe, mass_fe, mass_si, work);
+    gi::diag_fin1<<<1, 32, 0, s>>>(work, nblocks, out_dev);
+    gi::diag_pass2<<<nblocks, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n,
+                                           run.nfe, mass_fe, mass_si, out_dev, work);
+    gi::diag_fin2<<<1, 32, 0, s>>>(work, nblocks, out_dev);
+    return cudaGetLastError();
+}
+
+cudaError_t gi_launch_potential(const float4 *pos, const LaunchTable &tab,
+                                double *per_block, int nblocks, cudaStream_t s)
+{
+    if (nblocks <= 0) return cudaSuccess;
+    gi::potential_kernel<<<nblocks, GI_NT, 0, s>>>(pos, tab, per_block);
+    return cudaGetLastError();
+}
+
+cudaError_t gi_launch_ffma_peak(float *sink, int blocks, int iters, cudaStream_t s)
+{
+    gi::ffma_peak_kernel<<<blocks, 256, 0, s>>>(sink, iters);
+    return cudaGetLastError();
+}

@@ -1,0 +1,91 @@
+// gi_internal.h -- device-side tables and launch plumbing shared by the
+// libgi translation units.  Not part of the public ABI (see include/gi_api.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/gi_api.h"
+
+// Threads per CTA of the force kernels; also the j-tile staged in shared
+// memory and the granularity of the Kahan fold (one fold per 128 j).
+#define GI_NT 128
+// Runs and pair tables carried by value in one launch.
+#define GI_MAX_RUNS 64
+#define GI_MAX_PARAMS 8
+// Padding position for j beyond a chunk / i beyond a run: far enough that
+// gravity underflows to zero, never within contact range of a real body.
+#define GI_FAR_J 1.0e16f
+#define GI_FAR_I (-1.0e16f)
+
+#define GI_ACC_KAHAN GI_ACCUM_KAHAN
+#define GI_ACC_FP32 GI_ACCUM_FP32
+#define GI_ACC_FP64 GI_ACCUM_FP64
+
+#define GI_EPI_FORCE 0  // write force[i].xyz
+#define GI_EPI_STEP 1   // fused kick-drift into the other state buffer
+
+// Pair constants indexed by the pair class test = (i is Fe) + (j is Fe):
+// 0 = Si-Si, 1 = Fe-Si, 2 = Fe-Fe.
+struct PairDev {
+    float gm_fe, gm_si;  // sqrt(G) m: G m_i m_j = gm_i gm_j (far-field gravity)
+    float G[3];          // G m_i m_j of the class (contact band)
+    float K[3];          // full stiffness
+    float KRmid[3];      // reduced stiffness, middle shell band (Fe-Si: KRMix)
+    float KRin[3];       // reduced stiffness, inner band
+    float Tband[3];      // r >= ShellBreak(1)  <=>  r2 >= Tband
+    float Tmid[3];       // r >= ShellBreakFeSi2 <=> r2 >= Tmid (= Tband otherwise)
+};
+
+struct RunDev {
+    int offset, n, nfe, param;
+    int item_start;   // first work item of this run
+    int nsplit;       // j-chunks per i-block
+    int jchunk;       // bodies per j-chunk (multiple of GI_NT)
+    int nib;          // i-blocks
+    int tick_base;    // first ticket of this run
+    long long part_base;  // first double of this run's partial sums
+    float dt, dtm_fe, dtm_si, damp;
+    int ipt;          // i-bodies per thread this run was planned for
+};
+
+struct LaunchTable {
+    int nruns;
+    int nitems;
+    int sep_test;
+    int pad;
+    RunDev runs[GI_MAX_RUNS];
+    PairDev params[GI_MAX_PARAMS];
+};
+
+struct ForceArgs {
+    const float4 *pos;
+    const float4 *vel;
+    float4 *force;     // GI_EPI_FORCE
+    float4 *pos_out;   // GI_EPI_STEP
+    float4 *vel_out;   // GI_EPI_STEP
+    double *partials;  // split-j partial sums (nullptr when no run splits)
+    unsigned int *tickets;
+};
+
+// Launchers (gi_force_ipt*.cu).  Return cudaError_t of the launch.
+cudaError_t gi_launch_force(int ipt, int acc, int epi, const ForceArgs &a,
+                            const LaunchTable &tab, cudaStream_t s);
+cudaError_t gi_launch_force_ipt1(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, cudaStream_t s);
+cudaError_t gi_launch_force_ipt2(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, cudaStream_t s);
+cudaError_t gi_launch_force_ipt4(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, cudaStream_t s);
+// Resident CTAs per SM of a force kernel instance (for the planner).
+int gi_force_occupancy(int ipt, int acc, int epi);
+
+// gi_aux.cu
+cudaError_t gi_launch_move(float4 *pos, float4 *vel, const float4 *force,
+                           const LaunchTable &tab, cudaStream_t s);
+cudaError_t gi_launch_diag(const float4 *pos, const float4 *vel,
+                           const unsigned char *label, int scope,
+                           const RunDev &run, const PairDev &par, float mass_fe,
+                           float mass_si, double *work, int nblocks, double *out_dev,
+                           cudaStream_t s);
+cudaError_t gi_launch_potential(const float4 *pos, const LaunchTable &tab,
+                                double *per_block, int nblocks_per_run,
+                                cudaStream_t s);
+cudaError_t gi_launch_ffma_peak(float *sink, int blocks, int iters, cudaStream_t s);

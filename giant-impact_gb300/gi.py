@@ -1,0 +1,308 @@
+"""ctypes binding of libgi.so (include/gi_api.h) for Python callers.
+
+Every call goes through the C ABI; there is no Python or CPU fallback.  If
+libgi.so is missing or cannot run on this machine the calls raise GIError.
+Device pointers are plain integers (e.g. torch.Tensor.data_ptr()), streams
+are integers holding a cudaStream_t (0 = legacy default stream).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "lib", "libgi.so")
+HEADER = os.path.join(ROOT, "include", "gi_api.h")
+
+GI_OK = 0
+GI_SEP_REF_INT, GI_SEP_SIGN = 0, 1
+GI_ACCUM_KAHAN, GI_ACCUM_FP32, GI_ACCUM_FP64 = 0, 1, 2
+STATUS = {0: "GI_OK", 1: "GI_ERR_INVALID_ARG", 2: "GI_ERR_BAD_SIZE", 3: "GI_ERR_ALIGNMENT",
+          4: "GI_ERR_CUDA", 5: "GI_ERR_TIMEOUT", 6: "GI_ERR_NO_DEVICE", 7: "GI_ERR_OUT_OF_MEMORY",
+          8: "GI_ERR_PARAMS", 9: "GI_ERR_IO", 10: "GI_ERR_FORMAT", 11: "GI_ERR_CAPACITY"}
+
+
+class GIError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class PairParams(C.Structure):
+    _fields_ = [(n, C.c_float) for n in (
+        "GMassFeFe", "GMassFeSi", "GMassSiSi", "KFeFe", "KSiSi", "KFeSi", "KRFeFe", "KRSiSi",
+        "KRFeSi", "KRMix", "ShellBreakFe", "ShellBreakSi", "ShellBreakFeSi1", "ShellBreakFeSi2",
+        "MassFe", "MassSi")]
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Run(C.Structure):
+    _fields_ = [("offset", C.c_int), ("n", C.c_int), ("nfe", C.c_int), ("params", C.c_int),
+                ("dt", C.c_float), ("dt_over_mass_fe", C.c_float),
+                ("dt_over_mass_si", C.c_float), ("damp", C.c_float)]
+
+
+class Options(C.Structure):
+    _fields_ = [("sep_test", C.c_int), ("accum", C.c_int)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("i_per_thread", C.c_int), ("jchunk", C.c_int)]
+
+
+_FC = ["GMassFeFe", "GMassFeSi", "KFeFe", "KSiSi", "KFeSi", "KRFeFe", "KRSiSi", "KRFeSi",
+       "KRMix", "ShellBreakFe", "ShellBreakSi", "ShellBreakFeSi1", "ShellBreakFeSi2"]
+
+
+class ForceCollisionConsts(C.Structure):
+    _fields_ = [(n, C.c_float) for n in _FC] + [("NFe", C.c_int)]
+
+
+class MoveCollisionConsts(C.Structure):
+    _fields_ = [("Dt", C.c_float), ("DtOverMassFe", C.c_float), ("DtOverMassSi", C.c_float),
+                ("NFe", C.c_int)]
+
+
+class ForceSeparateConsts(C.Structure):
+    _fields_ = [(n, C.c_float) for n in _FC] + [("boarder1", C.c_int), ("boarder2", C.c_int),
+                                                 ("boarder3", C.c_int)]
+
+
+class MoveSeparateConsts(C.Structure):
+    _fields_ = [("Dt", C.c_float), ("DtOverMassFe", C.c_float), ("DtOverMassSi", C.c_float),
+                ("boarder1", C.c_int), ("boarder2", C.c_int), ("boarder3", C.c_int)]
+
+
+_P = C.c_void_p
+_SIGS = {
+    "gi_version": ([], C.c_int),
+    "gi_status_string": ([C.c_int], C.c_char_p),
+    "gi_last_error": ([], C.c_char_p),
+    "gi_device_info": ([C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                        C.POINTER(C.c_longlong)], C.c_int),
+    "gi_forces_collision": ([_P, _P, _P, C.POINTER(ForceCollisionConsts), C.c_int, _P], C.c_int),
+    "gi_move_collision": ([_P, _P, _P, C.POINTER(MoveCollisionConsts), C.c_int, _P], C.c_int),
+    "gi_forces_separate": ([_P, _P, _P, C.POINTER(ForceSeparateConsts), C.c_int, _P], C.c_int),
+    "gi_move_damped_separate": ([_P, _P, _P, C.POINTER(MoveSeparateConsts), C.c_float,
+                                 C.c_float, C.c_int, _P], C.c_int),
+    "gi_ctx_create": ([C.POINTER(_P), C.c_int], C.c_int),
+    "gi_ctx_destroy": ([_P], C.c_int),
+    "gi_ctx_set_options": ([_P, C.POINTER(Options)], C.c_int),
+    "gi_ctx_set_tuning": ([_P, C.POINTER(Tuning)], C.c_int),
+    "gi_ctx_get_tuning": ([_P, C.c_int, C.POINTER(Tuning)], C.c_int),
+    "gi_forces": ([_P, _P, _P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams), C.c_int, _P],
+                  C.c_int),
+    "gi_move": ([_P, _P, _P, _P, C.POINTER(Run), C.c_int, _P], C.c_int),
+    "gi_step": ([_P, _P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams), C.c_int, C.c_int,
+                 _P], C.c_int),
+    "gi_diag_fp64": ([_P, _P, _P, _P, C.c_int, C.POINTER(Run), C.POINTER(PairParams),
+                      C.POINTER(C.c_double), _P], C.c_int),
+    "gi_potential_fp64": ([_P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams), C.c_int,
+                           C.POINTER(C.c_double), _P], C.c_int),
+    "gi_run_host": ([_P, _P, _P, C.c_int, C.POINTER(Run), C.c_int, C.POINTER(PairParams),
+                     C.c_int, C.c_int, _P], C.c_int),
+    "gi_measure_ffma_peak": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
+    "gi_params_from_material": ([C.c_double] * 10 + [C.POINTER(PairParams)], C.c_int),
+    "gi_params_from_collision_consts": ([C.POINTER(ForceCollisionConsts), C.POINTER(PairParams)],
+                                        C.c_int),
+    "gi_ic_uniform_ball": ([C.c_ulonglong, C.c_int, C.c_double, C.c_double, C.c_float, C.c_float,
+                            C.c_float, C.c_float, _P, _P, C.POINTER(C.c_int)], C.c_int),
+    "gi_ic_lattice": ([C.c_ulonglong, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
+                       C.c_float, C.c_float, _P, _P], C.c_int),
+}
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load libgi.so (built by __graft_entry__.build()); raise if absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise GIError(6, f"{LIB_PATH} is not built; run __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        for name, (args, res) in _SIGS.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def header_symbols() -> list[str]:
+    """Names of every function declared in include/gi_api.h."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gi_[a-z0-9_]+)\s*\(", text)))
+
+
+def check(status: int) -> None:
+    if status != GI_OK:
+        raise GIError(status, lib().gi_last_error().decode(errors="replace"))
+
+
+def _arr(structs, cls):
+    if isinstance(structs, cls):
+        structs = [structs]
+    structs = list(structs)
+    a = (cls * max(1, len(structs)))(*structs)
+    return a, len(structs)
+
+
+def params_from_material(G=1.0, diameter=1.0, mass_fe=1.0, mass_si=0.4, k_fe=5.0, k_si=1.5,
+                         kr_fe=0.02, kr_si=0.01, sd_fe=0.002, sd_si=0.001) -> PairParams:
+    p = PairParams()
+    check(lib().gi_params_from_material(G, diameter, mass_fe, mass_si, k_fe, k_si, kr_fe, kr_si,
+                                        sd_fe, sd_si, C.byref(p)))
+    return p
+
+
+def params_from_collision_consts(c: ForceCollisionConsts) -> PairParams:
+    p = PairParams()
+    check(lib().gi_params_from_collision_consts(C.byref(c), C.byref(p)))
+    return p
+
+
+def collision_consts(p: PairParams, nfe: int) -> ForceCollisionConsts:
+    """Reference force struct from a pair table (the table's Si-Si gravity
+    must be 1, as the reference kernel assumes)."""
+    c = ForceCollisionConsts()
+    for n in _FC:
+        setattr(c, n, getattr(p, n))
+    c.NFe = nfe
+    return c
+
+
+def separate_consts(p: PairParams, b1: int, b2: int, b3: int) -> ForceSeparateConsts:
+    c = ForceSeparateConsts()
+    for n in _FC:
+        setattr(c, n, getattr(p, n))
+    c.boarder1, c.boarder2, c.boarder3 = b1, b2, b3
+    return c
+
+
+def device_info(device: int = 0) -> dict:
+    sm, ma, mi, mem = C.c_int(), C.c_int(), C.c_int(), C.c_longlong()
+    check(lib().gi_device_info(device, C.byref(sm), C.byref(ma), C.byref(mi), C.byref(mem)))
+    return {"sm_count": sm.value, "cc": (ma.value, mi.value), "mem_bytes": mem.value}
+
+
+def measure_ffma_peak(device: int = 0) -> float:
+    t = C.c_double()
+    check(lib().gi_measure_ffma_peak(device, C.byref(t)))
+    return t.value
+
+
+def forces_collision(pos, vel, force, consts, n, stream=0):
+    check(lib().gi_forces_collision(pos, vel, force, C.byref(consts), n, stream))
+
+
+def move_collision(pos, vel, force, consts, n, stream=0):
+    check(lib().gi_move_collision(pos, vel, force, C.byref(consts), n, stream))
+
+
+def forces_separate(pos, vel, force, consts, n, stream=0):
+    check(lib().gi_forces_separate(pos, vel, force, C.byref(consts), n, stream))
+
+
+def move_damped_separate(pos, vel, force, consts, damp1, damp2, n, stream=0):
+    check(lib().gi_move_damped_separate(pos, vel, force, C.byref(consts), damp1, damp2, n, stream))
+
+
+class Context:
+    """Owns a gi_ctx (scratch, options, tuning) on one device."""
+
+    def __init__(self, device: int = 0, sep_test: int = GI_SEP_REF_INT,
+                 accum: int = GI_ACCUM_KAHAN):
+        h = C.c_void_p()
+        check(lib().gi_ctx_create(C.byref(h), device))
+        self.h = h
+        self.set_options(sep_test, accum)
+
+    def close(self):
+        if self.h:
+            lib().gi_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_options(self, sep_test=GI_SEP_REF_INT, accum=GI_ACCUM_KAHAN):
+        o = Options(sep_test, accum)
+        check(lib().gi_ctx_set_options(self.h, C.byref(o)))
+
+    def set_tuning(self, i_per_thread=None, jchunk=0):
+        if i_per_thread is None:
+            check(lib().gi_ctx_set_tuning(self.h, None))
+        else:
+            t = Tuning(i_per_thread, jchunk)
+            check(lib().gi_ctx_set_tuning(self.h, C.byref(t)))
+
+    def get_tuning(self, n: int) -> tuple[int, int]:
+        t = Tuning()
+        check(lib().gi_ctx_get_tuning(self.h, n, C.byref(t)))
+        return t.i_per_thread, t.jchunk
+
+    def forces(self, pos, vel, force, runs, params, stream=0):
+        ra, nr = _arr(runs, Run)
+        pa, npar = _arr(params, PairParams)
+        check(lib().gi_forces(self.h, pos, vel, force, ra, nr, pa, npar, stream))
+
+    def move(self, pos, vel, force, runs, stream=0):
+        ra, nr = _arr(runs, Run)
+        check(lib().gi_move(self.h, pos, vel, force, ra, nr, stream))
+
+    def step(self, pos, vel, runs, params, nsteps, stream=0):
+        ra, nr = _arr(runs, Run)
+        pa, npar = _arr(params, PairParams)
+        check(lib().gi_step(self.h, pos, vel, ra, nr, pa, npar, nsteps, stream))
+
+    def diag(self, pos, vel, run, params, label=None, scope=0, stream=0) -> list[float]:
+        out = (C.c_double * 15)()
+        check(lib().gi_diag_fp64(self.h, pos, vel, label, scope, C.byref(run), C.byref(params),
+                                 out, stream))
+        return list(out)
+
+    def potential(self, pos, runs, params, stream=0) -> list[float]:
+        ra, nr = _arr(runs, Run)
+        pa, npar = _arr(params, PairParams)
+        out = (C.c_double * max(1, nr))()
+        check(lib().gi_potential_fp64(self.h, pos, ra, nr, pa, npar, out, stream))
+        return list(out[:nr])
+
+    def run_host(self, pos_host, vel_host, ntotal, runs, params, nsteps, stream=0):
+        ra, nr = _arr(runs, Run)
+        pa, npar = _arr(params, PairParams)
+        check(lib().gi_run_host(self.h, pos_host, vel_host, ntotal, ra, nr, pa, npar, nsteps,
+                                stream))
+
+
+def ic_uniform_ball(seed, n, radius=20.0, fe_fraction=0.3, mass_fe=1.0, mass_si=0.4,
+                    tag_fe=0.0, tag_si=1.0):
+    """Returns (pos, vel, nfe) as numpy float32 arrays of shape (n, 4)."""
+    import numpy as np
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    nfe = C.c_int()
+    check(lib().gi_ic_uniform_ball(seed, n, radius, fe_fraction, mass_fe, mass_si, tag_fe, tag_si,
+                                   pos.ctypes.data, vel.ctypes.data, C.byref(nfe)))
+    return pos, vel, nfe.value
+
+
+def ic_lattice(seed, n, spacing=0.999, jitter=0.004, vel_sigma=1.0, nfe=None, mass_fe=1.0,
+               mass_si=0.4):
+    import numpy as np
+    if nfe is None:
+        nfe = n // 3
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    check(lib().gi_ic_lattice(seed, n, spacing, jitter, vel_sigma, nfe, mass_fe, mass_si,
+                              pos.ctypes.data, vel.ctypes.data))
+    return pos, vel, nfe

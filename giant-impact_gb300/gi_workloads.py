@@ -1,0 +1,132 @@
+"""Seeded synthetic workloads with the shapes of the Giant-Impact runs.
+
+  config1(...)   8,192 bodies uniform in a ball of radius 20 D, inner 30 % by
+                 radius Fe; mFe = 1, mSi = 0.4, KFe = 5, KSi = 1.5,
+                 KR 0.02 / 0.01, shell depth 0.002 / 0.001 D; v = 0; dt = 1e-3.
+  impact(...)    two-body impact: target (60,000) and impactor (6,000), each
+                 built as a seeded ball and settled on the GPU with the damped
+                 separate-body step (the reference's generate-target-impactor
+                 damping phase, generateTargetImpactor.cu:666-749), spun about
+                 z at a fraction of breakup, placed at 45 degrees and moving at
+                 1.2 x the mutual escape speed, reordered [Fe1, Fe2, Si1, Si2]
+                 (impactInitialization.cu:329-371).
+Code units: G = 1, particle diameter D = 1.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+MATERIAL = dict(G=1.0, diameter=1.0, mass_fe=1.0, mass_si=0.4, k_fe=5.0, k_si=1.5, kr_fe=0.02,
+                kr_si=0.01, sd_fe=0.002, sd_si=0.001)
+DT = 1e-3
+
+
+def params(gi):
+    m = MATERIAL
+    return gi.params_from_material(m["G"], m["diameter"], m["mass_fe"], m["mass_si"], m["k_fe"],
+                                   m["k_si"], m["kr_fe"], m["kr_si"], m["sd_fe"], m["sd_si"])
+
+
+def run_desc(gi, offset, n, nfe, damp=0.0, dt=DT):
+    m = MATERIAL
+    return gi.Run(offset, n, nfe, 0, dt, dt / m["mass_fe"], dt / m["mass_si"], damp)
+
+
+def config1(gi, seed=1, n=8192, radius=20.0):
+    pos, vel, nfe = gi.ic_uniform_ball(seed, n, radius, 0.3, MATERIAL["mass_fe"],
+                                       MATERIAL["mass_si"], 0.0, 1.0)
+    return pos, vel, nfe
+
+
+def body_mass(n, nfe):
+    return nfe * MATERIAL["mass_fe"] + (n - nfe) * MATERIAL["mass_si"]
+
+
+def raw_body(gi, seed, n, tag_fe, tag_si):
+    """Seeded ball at ~50 % volume fraction, Fe inner 30 % by radius."""
+    radius = (n / 4.0) ** (1.0 / 3.0)
+    return gi.ic_uniform_ball(seed, n, radius, 0.3, MATERIAL["mass_fe"], MATERIAL["mass_si"],
+                              tag_fe, tag_si)
+
+
+def settle_pair(gi, torch, n_t, n_i, seed=2, steps=1500, damp=8.0, ctx=None):
+    """Build and settle target and impactor together on the GPU (separate
+    runs: no cross-body forces), reference order [Fe1, Si1, Fe2, Si2]."""
+    pt, vt, fet = raw_body(gi, seed, n_t, 0.0, 1.0)
+    pi, vi, fei = raw_body(gi, seed + 1000, n_i, 2.0, 3.0)
+    pos = np.concatenate([pt, pi])
+    vel = np.concatenate([vt, vi])
+    own = ctx is None
+    if own:
+        ctx = gi.Context(0)
+    p = params(gi)
+    runs = [run_desc(gi, 0, n_t, fet, damp), run_desc(gi, n_t, n_i, fei, damp)]
+    dp = torch.from_numpy(pos).cuda()
+    dv = torch.from_numpy(vel).cuda()
+    ctx.step(dp.data_ptr(), dv.data_ptr(), runs, p, steps)
+    # a short undamped rest, as in the reference's rest phase
+    runs0 = [run_desc(gi, 0, n_t, fet, 0.0), run_desc(gi, n_t, n_i, fei, 0.0)]
+    ctx.step(dp.data_ptr(), dv.data_ptr(), runs0, p, max(1, steps // 10))
+    torch.cuda.synchronize()
+    pos, vel = dp.cpu().numpy(), dv.cpu().numpy()
+    if own:
+        ctx.close()
+    return pos, vel, fet, fei
+
+
+def _com(pos, vel, n0, n, nfe):
+    m = np.where(np.arange(n) < nfe, MATERIAL["mass_fe"], MATERIAL["mass_si"])
+    x = pos[n0:n0 + n, :3].astype(np.float64)
+    v = vel[n0:n0 + n, :3].astype(np.float64)
+    M = m.sum()
+    return (m[:, None] * x).sum(0) / M, (m[:, None] * v).sum(0) / M, M
+
+
+def spin_and_place(pos, vel, n_t, n_i, fet, fei, spin_fraction=0.5, angle_deg=45.0,
+                   speed_factor=1.2, spin_t=None, spin_i=None):
+    """Zero each body's drift, spin about z, place the impactor at the given
+    impact angle and speed, reorder to [Fe1, Fe2, Si1, Si2].  Returns
+    (pos, vel, nfe_total)."""
+    pos = pos.astype(np.float64).copy()
+    vel = vel.astype(np.float64).copy()
+    radii = []
+    masses = []
+    for (n0, n, nfe), frac in (((0, n_t, fet), spin_t if spin_t is not None else spin_fraction),
+                               ((n_t, n_i, fei), spin_i if spin_i is not None else spin_fraction)):
+        c, v, M = _com(pos.astype(np.float32), vel.astype(np.float32), n0, n, nfe)
+        pos[n0:n0 + n, :3] -= c
+        vel[n0:n0 + n, :3] -= v
+        r = np.linalg.norm(pos[n0:n0 + n, :3], axis=1)
+        R = float(np.percentile(r, 99.0)) + 0.5
+        w = frac * math.sqrt(MATERIAL["G"] * M / R**3)
+        vel[n0:n0 + n, 0] += -w * pos[n0:n0 + n, 1]
+        vel[n0:n0 + n, 1] += w * pos[n0:n0 + n, 0]
+        radii.append(R)
+        masses.append(M)
+    Rt, Ri = radii
+    Mt, Mi = masses
+    d = Rt + Ri
+    vesc = math.sqrt(2 * MATERIAL["G"] * (Mt + Mi) / d)
+    b = d * math.sin(math.radians(angle_deg))
+    start = 1.25 * d
+    pos[n_t:, 0] += -start
+    pos[n_t:, 1] += b
+    vel[n_t:, 0] += speed_factor * vesc
+    # centre-of-mass frame
+    M = Mt + Mi
+    c_i = np.array([-start, b, 0.0])
+    v_i = np.array([speed_factor * vesc, 0.0, 0.0])
+    pos[:, :3] -= (Mi * c_i) / M
+    vel[:, :3] -= (Mi * v_i) / M
+    # reorder [Fe1, Si1, Fe2, Si2] -> [Fe1, Fe2, Si1, Si2]
+    order = np.concatenate([np.arange(0, fet), np.arange(n_t, n_t + fei), np.arange(fet, n_t),
+                            np.arange(n_t + fei, n_t + n_i)])
+    return (pos[order].astype(np.float32), vel[order].astype(np.float32), fet + fei)
+
+
+def impact(gi, torch, n_t=60000, n_i=6000, seed=2, settle_steps=1500, spin_fraction=0.5,
+           angle_deg=45.0, speed_factor=1.2, ctx=None):
+    pos, vel, fet, fei = settle_pair(gi, torch, n_t, n_i, seed=seed, steps=settle_steps, ctx=ctx)
+    return spin_and_place(pos, vel, n_t, n_i, fet, fei, spin_fraction, angle_deg, speed_factor)

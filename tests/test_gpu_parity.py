@@ -1,0 +1,338 @@
+"""GPU parity tests: libgi's sm_103a kernels, called through the C ABI, against
+the FP64 oracle, the reference-exact CPU restatement and the reference's own
+CUDA kernels on identical seeded inputs.
+
+Tolerances (force): global relative L2 error against the FP64 oracle
+<= 1e-5 (the stated force-error bound), and against the reference's own
+kernels <= 1e-5.  Kick-drift: bit-exact.  Integer/index work (run
+decomposition, batch invariance): bit-exact."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import config1_params, reference_unit_params, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FORCE_TOL = 1e-5
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    return t.cpu().numpy()
+
+
+def stream(torch):
+    return torch.cuda.current_stream().cuda_stream
+
+
+@pytest.fixture(scope="module")
+def ctx(gi, torch_cuda):
+    c = gi.Context(0)
+    yield c
+    c.close()
+
+
+def gpu_forces(gi, torch, ctx, pos, vel, runs, params):
+    dp, dv = dev(torch, pos), dev(torch, vel)
+    df = torch.full_like(dp, float("nan"))
+    ctx.forces(dp.data_ptr(), dv.data_ptr(), df.data_ptr(), runs, params, stream(torch))
+    torch.cuda.synchronize()
+    return host(df)
+
+
+def ball_with_velocities(gi, n, seed, vscale=1.5):
+    pos, vel, nfe = gi.ic_uniform_ball(seed, n, 20.0 * (n / 8192.0) ** (1 / 3), 0.3, 1.0, 0.4,
+                                       0.0, 1.0)
+    rng = np.random.default_rng(seed)
+    vel[:, :3] = rng.normal(scale=vscale, size=(n, 3)).astype(np.float32)
+    return pos, vel, nfe
+
+
+def test_config1_force_vs_fp64(gi, orc, torch_cuda, ctx):
+    """The 8,192-body settle workload: per-step force error vs FP64."""
+    import gi_workloads as wl
+    pos, vel, nfe = wl.config1(gi)
+    p = wl.params(gi)
+    run = wl.run_desc(gi, 0, len(pos), nfe)
+    f = gpu_forces(gi, torch_cuda, ctx, pos, vel, [run], p)
+    f64, absf = orc.forces_fp64(pos, vel, [run], p)
+    err = rel_l2(f[:, :3], f64)
+    per_body = np.abs(f[:, :3] - f64).max(1) / absf
+    print(f"config1 rel L2 {err:.3e}, max per-body err / sum|f| {per_body.max():.3e}")
+    assert err < FORCE_TOL
+    assert per_body.max() < 1e-5
+    assert np.all(np.isnan(f[:, 3]))  # .w untouched
+
+
+@pytest.mark.parametrize("kind", ["lattice", "ball"])
+def test_drop_in_collision_vs_reference_kernel(gi, orc, torch_cuda, kind):
+    """gi_forces_collision vs the reference's getForcesCollisionSingleGPU on
+    the same inputs (reference units, N a multiple of 256)."""
+    torch = torch_cuda
+    p = reference_unit_params(gi)
+    if kind == "lattice":
+        pos, vel, nfe = gi.ic_lattice(7, 4096, spacing=0.999, jitter=0.004, vel_sigma=2.0,
+                                      mass_fe=p.MassFe, mass_si=p.MassSi)
+    else:
+        pos, vel, nfe = ball_with_velocities(gi, 8192, 8)
+    n = len(pos)
+    c = gi.collision_consts(p, nfe)
+    dp, dv = dev(torch, pos), dev(torch, vel)
+    mine = torch.full_like(dp, float("nan"))
+    theirs = torch.full_like(dp, float("nan"))
+    gi.forces_collision(dp.data_ptr(), dv.data_ptr(), mine.data_ptr(), c, n, stream(torch))
+    ref = orc.ref_lib()
+    if ref is None:
+        pytest.skip("reference kernels not built (oracle/_ref absent)")
+    assert ref.giref_forces_collision(dp.data_ptr(), dv.data_ptr(), theirs.data_ptr(), C.byref(c),
+                                      n, stream(torch)) == 0
+    torch.cuda.synchronize()
+    mine, theirs = host(mine)[:, :3], host(theirs)[:, :3]
+    run = (0, n, nfe, 0, 0, 0, 0, 0)
+    f64, _ = orc.forces_fp64(pos, vel, [run], p)
+    e_mine, e_ref, e_mr = rel_l2(mine, f64), rel_l2(theirs, f64), rel_l2(mine, theirs)
+    print(f"{kind}: mine vs fp64 {e_mine:.3e}, reference vs fp64 {e_ref:.3e}, mine vs ref {e_mr:.3e}")
+    assert e_mine < FORCE_TOL
+    assert e_mr < FORCE_TOL
+    # the reference-exact oracle reproduces the reference kernel
+    assert np.array_equal(orc.forces_ref(pos, vel, [run], p)[:, :3], theirs)
+
+
+def test_drop_in_separate_vs_reference_kernel(gi, orc, torch_cuda):
+    torch = torch_cuda
+    p = reference_unit_params(gi)
+    pa, va, fa = gi.ic_lattice(21, 3072, vel_sigma=1.5, nfe=1000, mass_fe=p.MassFe, mass_si=p.MassSi)
+    pb, vb, fb = gi.ic_lattice(22, 1024, vel_sigma=1.5, nfe=300, mass_fe=p.MassFe, mass_si=p.MassSi)
+    pb[:, 0] += 4.0
+    pos, vel = np.concatenate([pa, pb]), np.concatenate([va, vb])
+    n, b1, b2, b3 = 4096, fa, 3072, 3072 + fb
+    sc = gi.separate_consts(p, b1, b2, b3)
+    dp, dv = dev(torch, pos), dev(torch, vel)
+    mine = torch.zeros_like(dp)
+    gi.forces_separate(dp.data_ptr(), dv.data_ptr(), mine.data_ptr(), sc, n, stream(torch))
+    torch.cuda.synchronize()
+    runs = [(0, b2, b1, 0, 0, 0, 0, 0), (b2, n - b2, b3 - b2, 0, 0, 0, 0, 0)]
+    f64, _ = orc.forces_fp64(pos, vel, runs, p)
+    assert rel_l2(host(mine)[:, :3], f64) < FORCE_TOL
+    ref = orc.ref_lib()
+    if ref is None:
+        pytest.skip("reference kernels not built")
+    theirs = torch.zeros_like(dp)
+    assert ref.giref_forces_separate(dp.data_ptr(), dv.data_ptr(), theirs.data_ptr(), C.byref(sc),
+                                     n, stream(torch)) == 0
+    torch.cuda.synchronize()
+    assert rel_l2(host(mine)[:, :3], host(theirs)[:, :3]) < FORCE_TOL
+
+
+def test_move_bitwise_vs_reference_kernel(gi, orc, torch_cuda):
+    torch = torch_cuda
+    rng = np.random.default_rng(3)
+    n, nfe = 2048, 700
+    pos = rng.normal(size=(n, 4)).astype(np.float32)
+    vel = rng.normal(size=(n, 4)).astype(np.float32)
+    force = rng.normal(size=(n, 4)).astype(np.float32) * 50
+    mc = gi.MoveCollisionConsts(6.3e-4, 6.3e-4 / 2.5, 6.3e-4, nfe)
+    a = [dev(torch, x) for x in (pos, vel, force)]
+    gi.move_collision(a[0].data_ptr(), a[1].data_ptr(), a[2].data_ptr(), mc, n, stream(torch))
+    torch.cuda.synchronize()
+    run = (0, n, nfe, 0, mc.Dt, mc.DtOverMassFe, mc.DtOverMassSi, 0.0)
+    p2, v2 = orc.move_ref(pos, vel, force, [run])
+    assert np.array_equal(host(a[0]), p2) and np.array_equal(host(a[1]), v2)
+    ref = orc.ref_lib()
+    if ref is not None:
+        b = [dev(torch, x) for x in (pos, vel, force)]
+        assert ref.giref_move_collision(b[0].data_ptr(), b[1].data_ptr(), b[2].data_ptr(),
+                                        C.byref(mc), n, stream(torch)) == 0
+        torch.cuda.synchronize()
+        assert np.array_equal(host(a[0]), host(b[0])) and np.array_equal(host(a[1]), host(b[1]))
+    # damped, two bodies
+    ms = gi.MoveSeparateConsts(1e-3, 1e-3, 2.5e-3, 300, 1500, 1800)
+    c = [dev(torch, x) for x in (pos, vel, force)]
+    gi.move_damped_separate(c[0].data_ptr(), c[1].data_ptr(), c[2].data_ptr(), ms, 8.0, 2.0, n,
+                            stream(torch))
+    torch.cuda.synchronize()
+    runs = [(0, 1500, 300, 0, 1e-3, 1e-3, 2.5e-3, 8.0), (1500, 548, 300, 0, 1e-3, 1e-3, 2.5e-3, 2.0)]
+    p3, v3 = orc.move_ref(pos, vel, force, runs)
+    assert np.array_equal(host(c[0]), p3) and np.array_equal(host(c[1]), v3)
+    if ref is not None:
+        d = [dev(torch, x) for x in (pos, vel, force)]
+        assert ref.giref_move_damped_separate(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr(),
+                                              C.byref(ms), 8.0, 2.0, n, stream(torch)) == 0
+        torch.cuda.synchronize()
+        assert np.array_equal(host(c[1]), host(d[1]))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 127, 128, 129, 255, 257, 1000, 4099])
+def test_ragged_sizes(gi, orc, torch_cuda, ctx, n):
+    p = config1_params(gi)
+    pos, vel, nfe = gi.ic_lattice(n, n, spacing=0.999, jitter=0.004, vel_sigma=1.0, nfe=n // 3)
+    run = (0, n, nfe, 0, 0.0, 0.0, 0.0, 0.0)
+    f = gpu_forces(gi, torch_cuda, ctx, pos, vel, [gi.Run(*run)], p)
+    f64, absf = orc.forces_fp64(pos, vel, [run], p)
+    if n == 1:
+        assert np.all(f[:, :3] == 0)
+    else:
+        assert rel_l2(f[:, :3], f64) < FORCE_TOL
+        assert np.all(np.abs(f[:, :3] - f64).max(1) <= 1e-5 * absf + 1e-30)
+
+
+def test_empty_and_invalid(gi, torch_cuda, ctx):
+    torch = torch_cuda
+    p = config1_params(gi)
+    dp = torch.zeros((16, 4), device="cuda")
+    # empty run: no-op
+    ctx.forces(dp.data_ptr(), dp.data_ptr(), dp.data_ptr(), [gi.Run(0, 0, 0, 0, 0, 0, 0, 0)], p)
+    with pytest.raises(gi.GIError) as e:
+        ctx.forces(dp.data_ptr() + 4, dp.data_ptr(), dp.data_ptr(), [gi.Run(0, 8, 0, 0, 0, 0, 0, 0)], p)
+    assert e.value.status == 3
+    with pytest.raises(gi.GIError) as e:
+        ctx.forces(dp.data_ptr(), dp.data_ptr(), dp.data_ptr(),
+                   [gi.Run(0, 8, 0, 0, 0, 0, 0, 0), gi.Run(4, 8, 0, 0, 0, 0, 0, 0)], p)
+    assert e.value.status == 1
+    with pytest.raises(gi.GIError) as e:
+        ctx.forces(dp.data_ptr(), dp.data_ptr(), dp.data_ptr(), [gi.Run(0, 8, 9, 0, 0, 0, 0, 0)], p)
+    assert e.value.status == 2
+    bad = gi.PairParams.from_buffer_copy(bytes(p))
+    bad.GMassFeSi = 3.0 * bad.GMassFeSi
+    with pytest.raises(gi.GIError) as e:
+        ctx.forces(dp.data_ptr(), dp.data_ptr(), dp.data_ptr(), [gi.Run(0, 8, 2, 0, 0, 0, 0, 0)], bad)
+    assert e.value.status == 8
+
+
+def test_fused_step_equals_force_then_move(gi, torch_cuda, ctx):
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    pos, vel, nfe = gi.ic_lattice(5, 6000, vel_sigma=1.0)
+    run = wl.run_desc(gi, 0, 6000, nfe)
+    dp, dv = dev(torch, pos), dev(torch, vel)
+    for _ in range(3):
+        df = torch.zeros_like(dp)
+        ctx.forces(dp.data_ptr(), dv.data_ptr(), df.data_ptr(), [run], p)
+        ctx.move(dp.data_ptr(), dv.data_ptr(), df.data_ptr(), [run])
+    ep, ev = dev(torch, pos), dev(torch, vel)
+    ctx.step(ep.data_ptr(), ev.data_ptr(), [run], p, 3)
+    torch.cuda.synchronize()
+    assert torch.equal(dp, ep) and torch.equal(dv, ev)
+
+
+def test_batch_invariance(gi, torch_cuda, ctx):
+    """A run's forces are bit-identical alone and inside a batch."""
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    sizes = [5000, 12000, 700, 33000]
+    bodies = [gi.ic_lattice(s + 1, s, vel_sigma=1.0) for s in sizes]
+    pos = np.concatenate([b[0] for b in bodies])
+    vel = np.concatenate([b[1] for b in bodies])
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(int)
+    runs = [wl.run_desc(gi, int(o), s, b[2]) for o, s, b in zip(offs, sizes, bodies)]
+    mixed = gpu_forces(gi, torch, ctx, pos, vel, runs, p)
+    for k, (o, s) in enumerate(zip(offs, sizes)):
+        alone = gpu_forces(gi, torch, ctx, bodies[k][0], bodies[k][1],
+                           [wl.run_desc(gi, 0, s, bodies[k][2])], p)
+        assert np.array_equal(alone[:, :3], mixed[o:o + s, :3]), k
+
+
+@pytest.mark.parametrize("ipt,jchunk", [(1, 0), (2, 1024), (4, 2048), (4, 128), (1, 384)])
+def test_decompositions_agree(gi, orc, torch_cuda, ctx, ipt, jchunk):
+    p = config1_params(gi)
+    pos, vel, nfe = gi.ic_lattice(9, 5000, vel_sigma=1.5)
+    run = gi.Run(0, 5000, nfe, 0, 0, 0, 0, 0)
+    ctx.set_tuning(ipt, jchunk)
+    try:
+        f = gpu_forces(gi, torch_cuda, ctx, pos, vel, [run], p)
+    finally:
+        ctx.set_tuning(None)
+    f64, _ = orc.forces_fp64(pos, vel, [(0, 5000, nfe, 0, 0, 0, 0, 0)], p)
+    assert rel_l2(f[:, :3], f64) < FORCE_TOL
+
+
+@pytest.mark.parametrize("accum", [0, 1, 2])
+def test_accumulation_modes(gi, orc, torch_cuda, accum):
+    p = config1_params(gi)
+    pos, vel, nfe = ball_with_velocities(gi, 20000, 4)
+    c = gi.Context(0, accum=accum)
+    run = gi.Run(0, len(pos), nfe, 0, 0, 0, 0, 0)
+    c.set_tuning(4, 0)  # one chunk: the accumulation mode alone decides the error
+    f = gpu_forces(gi, torch_cuda, c, pos, vel, [run], p)
+    c.close()
+    idx = np.arange(0, len(pos), 7)
+    f64, _ = orc.forces_fp64(pos, vel, [(0, len(pos), nfe, 0, 0, 0, 0, 0)], p, idx=idx)
+    err = rel_l2(f[idx, :3], f64)
+    print(f"accum {accum}: rel L2 {err:.3e}")
+    assert err < (2e-5 if accum == 1 else FORCE_TOL)
+
+
+def test_sign_separation_mode(gi, orc, torch_cuda):
+    p = config1_params(gi)
+    pos, vel, nfe = gi.ic_lattice(31, 3000, vel_sigma=0.3)
+    c = gi.Context(0, sep_test=gi.GI_SEP_SIGN)
+    f = gpu_forces(gi, torch_cuda, c, pos, vel, [gi.Run(0, 3000, nfe, 0, 0, 0, 0, 0)], p)
+    c.close()
+    run = (0, 3000, nfe, 0, 0, 0, 0, 0)
+    f64, _ = orc.forces_fp64(pos, vel, [run], p, sep_test=orc.SEP_SIGN)
+    f64_int, _ = orc.forces_fp64(pos, vel, [run], p, sep_test=orc.SEP_REF_INT)
+    assert rel_l2(f[:, :3], f64) < FORCE_TOL
+    assert rel_l2(f64_int, f64) > 1e-4  # the two tests really differ here
+
+
+def test_diag_and_potential_vs_oracle(gi, orc, torch_cuda, ctx):
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    pos, vel, nfe = ball_with_velocities(gi, 9000, 12)
+    run = wl.run_desc(gi, 0, 9000, nfe)
+    dp, dv = dev(torch, pos), dev(torch, vel)
+    d = np.array(ctx.diag(dp.data_ptr(), dv.data_ptr(), run, p))
+    want = orc.diag_fp64(pos, vel, (0, 9000, nfe, 0, 0, 0, 0, 0), p)
+    assert np.allclose(d, want, rtol=1e-12, atol=1e-9 * np.abs(want).max())
+    label = np.zeros(9000, np.uint8)
+    label[:4000] = 1
+    label[4000:5000] = 2
+    dl = dev(torch, label)
+    for scope in (1, 2, 3):
+        d = np.array(ctx.diag(dp.data_ptr(), dv.data_ptr(), run, p, label=dl.data_ptr(), scope=scope))
+        want = orc.diag_fp64(pos, vel, (0, 9000, nfe, 0, 0, 0, 0, 0), p, label=label, scope=scope)
+        assert np.allclose(d, want, rtol=1e-12, atol=1e-9 * np.abs(want).max()), scope
+    u = ctx.potential(dp.data_ptr(), [run], p)[0]
+    u64 = orc.potential_fp64(pos, [(0, 9000, nfe, 0, 0, 0, 0, 0)], p).sum() / 2
+    print(f"potential {u:.10e} vs {u64:.10e}")
+    assert u == pytest.approx(u64, rel=1e-7)
+
+
+def test_run_host_matches_device_path(gi, torch_cuda, ctx):
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    pos, vel, nfe = gi.ic_lattice(77, 3000, vel_sigma=1.0)
+    run = wl.run_desc(gi, 0, 3000, nfe)
+    hp, hv = pos.copy(), vel.copy()
+    ctx.run_host(hp.ctypes.data, hv.ctypes.data, 3000, [run], p, 4)
+    dp, dv = dev(torch, pos), dev(torch, vel)
+    ctx.step(dp.data_ptr(), dv.data_ptr(), [run], p, 4)
+    torch.cuda.synchronize()
+    assert np.array_equal(hp, host(dp)) and np.array_equal(hv, host(dv))
+
+
+def test_large_n_subsample_vs_fp64(gi, orc, torch_cuda, ctx):
+    """1,153,434 bodies (the precision-study size): FP64 oracle on a seeded
+    subsample of i-bodies against all j."""
+    n = 1_153_434
+    p = config1_params(gi)
+    pos, vel, nfe = gi.ic_uniform_ball(5, n, 20.0 * (n / 8192.0) ** (1 / 3), 0.3, 1.0, 0.4, 0.0, 1.0)
+    run = gi.Run(0, n, nfe, 0, 0, 0, 0, 0)
+    f = gpu_forces(gi, torch_cuda, ctx, pos, vel, [run], p)
+    idx = np.random.default_rng(5).choice(n, 96, replace=False).astype(np.int32)
+    f64, _ = orc.forces_fp64(pos, vel, [(0, n, nfe, 0, 0, 0, 0, 0)], p, idx=idx)
+    err = rel_l2(f[idx, :3], f64)
+    print(f"N={n}: subsample rel L2 {err:.3e}")
+    assert err < FORCE_TOL
+    assert np.isfinite(f[:, :3]).all()
