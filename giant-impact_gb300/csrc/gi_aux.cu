@@ -177,7 +177,7 @@ potential_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchT
         for (int jj = 0; jj < GI_NT; ++jj) {
             const float4 q = sP[jj];
             const float dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
-            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
             const bool c = r2 < 1.0f;
             // Contact pairs (and the self pair, r2 == 0) are taken out of the
             // far sum; rr keeps rsqrt finite for them.

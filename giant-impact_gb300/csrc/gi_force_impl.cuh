@@ -13,6 +13,10 @@
 // small runs still fill all SMs; a chunk is processed in tiles of GI_NT
 // bodies staged in shared memory and read back as broadcast LDS.128.
 //
+// r2 and dp.dv are formed as fma(z, z, fma(x, x, y*y)), the evaluation the
+// reference's own build uses, so band and K/KR decisions see the identical
+// FP32 r2 and dp.dv.
+//
 // Inner loop (per j, per i): 3 FADD, 1 FMUL + 2 FFMA (r2), MUFU.RSQ,
 // 3 FMUL (m_j r^-3), compare + select, 3 FFMA: far-field gravity only.
 // Pairs with r2 < 1 contribute zero there; when any lane of the warp has
@@ -31,6 +35,16 @@
 #include "gi_internal.h"
 
 namespace gi {
+
+// MUFU reciprocal square root (PTX rsqrt.approx.ftz.f32).  Only pairs with
+// r2 >= 1 use the value, so flushing denormal inputs changes nothing; r2 = 0
+// (the self pair) gives +inf, which the contact mask discards.
+__device__ __forceinline__ float rsqrt_mufu(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 
 __device__ __forceinline__ int find_run(const LaunchTable &tab, int item)
 {
@@ -69,7 +83,7 @@ __device__ __forceinline__ void contact_pair(const PairDev &P, int sep_test,
         const float4 vi = __ldg(&vel[i]);
         const float dvx = __fsub_rn(vj.x, vi.x), dvy = __fsub_rn(vj.y, vi.y),
                     dvz = __fsub_rn(vj.z, vi.z);
-        const float dpdv = __fmaf_rn(dz, dvz, __fmaf_rn(dy, dvy, __fmul_rn(dx, dvx)));
+        const float dpdv = __fmaf_rn(dz, dvz, __fmaf_rn(dx, dvx, __fmul_rn(dy, dvy)));
         // Reference: int inout = dp.dv; KR when inout > 0, i.e. dp.dv >= 1.
         const bool sep = (sep_test == GI_SEP_SIGN) ? (dpdv > 0.0f) : (dpdv >= 1.0f);
         if (sep) K = (r2 >= P.Tmid[test]) ? P.KRmid[test] : P.KRin[test];
@@ -160,36 +174,35 @@ force_kernel(const ForceArgs a, const __grid_constant__ LaunchTable tab)
 #pragma unroll 4
         for (int jj = 0; jj < GI_NT; ++jj) {
             const float4 q = sP[jj];
-            unsigned int cmask = 0u;
+            bool anyc = false;
 #pragma unroll
             for (int k = 0; k < IPT; ++k) {
                 const float dx = q.x - xi[k], dy = q.y - yi[k], dz = q.z - zi[k];
-                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
-                const float ri = rsqrtf(r2);
+                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+                const float ri = rsqrt_mufu(r2);
                 float s = ri * ri;
                 s = s * ri;
                 s = s * q.w;
                 const bool c = r2 < 1.0f;
                 s = c ? 0.0f : s;
-                cmask |= (c ? 1u : 0u) << k;
+                anyc = anyc || c;
                 tx[k] = __fmaf_rn(s, dx, tx[k]);
                 ty[k] = __fmaf_rn(s, dy, ty[k]);
                 tz[k] = __fmaf_rn(s, dz, tz[k]);
             }
-            if (__any_sync(0xffffffffu, cmask != 0u)) {
+            if (__any_sync(0xffffffffu, anyc)) {
                 const float4 vq = sV[jj];
                 const int jg = jt + jj;
 #pragma unroll
                 for (int k = 0; k < IPT; ++k) {
                     const int ig = i0 + k * GI_NT + tid;
+                    const float dx = q.x - xi[k], dy = q.y - yi[k], dz = q.z - zi[k];
+                    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
                     // Padding never reaches here (it sits 1e16 away), but the
                     // contact path loads vel[i]: keep it inside the run regardless.
-                    if ((cmask & (1u << k)) && ig < rend && jg < j1) {
-                        const float dx = q.x - xi[k], dy = q.y - yi[k], dz = q.z - zi[k];
-                        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+                    if (r2 < 1.0f && ig < rend && jg < j1)
                         contact_pair(P, tab.sep_test, ig, jg, sw, dx, dy, dz, r2, vel, vq,
                                      kx[k], ky[k], kz[k]);
-                    }
                 }
             }
         }

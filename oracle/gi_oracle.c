@@ -66,12 +66,18 @@ float gio_r2_threshold(float s)
 /* Reference-exact pair evaluation                                           */
 /* ------------------------------------------------------------------------ */
 
-/* r2 = dx*dx + dy*dy + dz*dz as nvcc evaluates it: ((dx*dx) + dy*dy) + dz*dz
- * with the two trailing products fused. */
+/* r2 = dx*dx + dy*dy + dz*dz as the reference's nvcc build evaluates it:
+ * each add is fused with the product that stands first in it, giving
+ * fma(dz, dz, fma(dx, dx, dy*dy)); pinned bit for bit against the golden
+ * vectors from the reference kernels (tests/golden). */
 static inline float dot3_ref(float ax, float ay, float az, float bx, float by,
                              float bz, int fused)
 {
-    if (fused) return fmaf(az, bz, fmaf(ay, by, ax * bx));
+    /* fused == 1: (a.x b.x + a.y b.y) + a.z b.z with both adds fused onto
+     * the product that stands first in each add: fma(az, bz, fma(ax, bx, ay*by)).
+     * fused == 2: the other pairing, fma(az, bz, fma(ay, by, ax*bx)). */
+    if (fused == 1) return fmaf(az, bz, fmaf(ax, bx, ay * by));
+    if (fused == 2) return fmaf(az, bz, fmaf(ay, by, ax * bx));
     float t = ax * bx;
     t = t + ay * by;
     return t + az * bz;
@@ -131,7 +137,10 @@ static void ref_body(const f4 *pos, const f4 *vel, int id, const gio_run *run,
                      const gio_params *c, int sep_test, int fma_mask,
                      float out[3])
 {
-    const int fuse_r2 = fma_mask & 1, fuse_dot = (fma_mask >> 1) & 1,
+    /* bit 4 selects the alternative pairing of the fused dot products */
+    const int alt = (fma_mask >> 4) & 1;
+    const int fuse_r2 = (fma_mask & 1) ? 1 + alt : 0,
+              fuse_dot = ((fma_mask >> 1) & 1) ? 1 + alt : 0,
               fuse_acc = (fma_mask >> 2) & 1;
     const f4 pi = pos[id];
     const f4 vi = vel[id];
