@@ -217,13 +217,25 @@ def run_ours(a):
     n = len(pos)
     p = wl.params(gi)
     run = wl.run_desc(gi, 0, n, nfe)
-    dp = torch.from_numpy(pos).cuda()
-    dv = torch.from_numpy(vel).cuda()
+    # two state buffers: step k reads one and writes the other (no copies)
+    bufs = [(torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda()),
+            (torch.empty((n, 4), dtype=torch.float32, device="cuda"),
+             torch.empty((n, 4), dtype=torch.float32, device="cuda"))]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
     stream = torch.cuda.current_stream()
     s = stream.cuda_stream
-    for _ in range(max(3, a.warmup)):
-        ctx.step(dp.data_ptr(), dv.data_ptr(), [run], p, 1, s)
+
+    def one_step(k):
+        (pa, va), (pb, vb) = bufs[k % 2], bufs[(k + 1) % 2]
+        ctx.step_pingpong(pa.data_ptr(), va.data_ptr(), pb.data_ptr(), vb.data_ptr(), [run], p, 1, s)
+
+    # autotune the decomposition for this N on these bodies (setup, untimed)
+    t_tune = time.perf_counter()
+    ctx.autotune(bufs[0][0].data_ptr(), bufs[0][1].data_ptr(), [run], p, s)
+    t_tune = time.perf_counter() - t_tune
+    nw = max(3, a.warmup)
+    for k in range(nw):
+        one_step(k)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
@@ -236,7 +248,7 @@ def run_ours(a):
     for k in range(a.steps):
         flush.fill_(float(k))
         evs[k][0].record(stream)
-        ctx.step(dp.data_ptr(), dv.data_ptr(), [run], p, 1, s)
+        one_step(nw + k)
         evs[k][1].record(stream)
     torch.cuda.synchronize()
     if world > 1:
@@ -252,6 +264,7 @@ def run_ours(a):
     ms = total_ms / a.steps
     inter = n * (n - 1)
     value = world * inter * a.steps / (total_ms * 1e-3)
+    dp, dv = bufs[(nw + a.steps) % 2]
     state_ok = bool(torch.isfinite(dp).all().item() and torch.isfinite(dv).all().item())
 
     # end-to-end through the host-buffer entry point (pinned memory, copies timed)
@@ -273,12 +286,13 @@ def run_ours(a):
         info = gi.device_info(local)
         achieved = inter * FLOP_PER_INTERACTION / (ms * 1e-3) / 1e12
         ipt, jchunk = ctx.get_tuning(n)
-        roof = {"bound": "fp32_ffma", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+        roof = {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": None,
                 "peak_source": "measured FFMA microbenchmark (gi_measure_ffma_peak) on this GPU "
                                "in this run; MEASURED_PEAKS.json has no FP32 figure",
                 "nominal_peak": info["sm_count"] * 128 * 2 * 2.07e9 / 1e12,
-                "kernel": f"gi::force_kernel<{ipt},KAHAN,STEP> (fused force + kick-drift)",
+                "kernel": f"gi::force_kernel<{ipt},KAHAN,STEP> (fused force + kick-drift), "
+                          f"one launch per step via gi_step_pingpong",
                 "flop_per_interaction": FLOP_PER_INTERACTION,
                 "interactions_per_launch": inter}
         cpu = None
@@ -296,7 +310,7 @@ def run_ours(a):
                                    "30% Fe, spin 0.5 breakup, 45 deg, 1.2 v_esc, dt 1e-3",
                        "n_bodies": n, "interactions_per_step": inter,
                        "accumulation": "kahan (FP32 tiles of 128, compensated across tiles)",
-                       "tuning": {"i_per_thread": ipt, "jchunk": jchunk},
+                       "tuning": {"i_per_thread": ipt, "jchunk": jchunk, "autotune_s": round(t_tune, 2)},
                        "l2": "flushed between timed steps (256 MB write, outside the events)",
                        "parallelism": f"replicas x{world}"},
             "fp32_tflops": achieved, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,

@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -15,6 +16,7 @@
 int gi_force_occupancy_ipt1(int acc, int epi);
 int gi_force_occupancy_ipt2(int acc, int epi);
 int gi_force_occupancy_ipt4(int acc, int epi);
+int gi_force_occupancy_ipt8(int acc, int epi);
 
 // ------------------------------------------------------------------ errors --
 
@@ -83,12 +85,13 @@ extern "C" int gi_device_info(int device, int *sm_count, int *cc_major, int *cc_
 }
 
 cudaError_t gi_launch_force(int ipt, int acc, int epi, const ForceArgs &a,
-                            const LaunchTable &tab, cudaStream_t s)
+                            const LaunchTable &tab, int grid, cudaStream_t s)
 {
     switch (ipt) {
-    case 1: return gi_launch_force_ipt1(acc, epi, a, tab, s);
-    case 2: return gi_launch_force_ipt2(acc, epi, a, tab, s);
-    case 4: return gi_launch_force_ipt4(acc, epi, a, tab, s);
+    case 1: return gi_launch_force_ipt1(acc, epi, a, tab, grid, s);
+    case 2: return gi_launch_force_ipt2(acc, epi, a, tab, grid, s);
+    case 4: return gi_launch_force_ipt4(acc, epi, a, tab, grid, s);
+    case 8: return gi_launch_force_ipt8(acc, epi, a, tab, grid, s);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -99,6 +102,7 @@ int gi_force_occupancy(int ipt, int acc, int epi)
     case 1: return gi_force_occupancy_ipt1(acc, epi);
     case 2: return gi_force_occupancy_ipt2(acc, epi);
     case 4: return gi_force_occupancy_ipt4(acc, epi);
+    case 8: return gi_force_occupancy_ipt8(acc, epi);
     default: return 0;
     }
 }
@@ -123,8 +127,8 @@ static int to_device_params(const gi_pair_params &p, PairDev &d)
                           p.ShellBreakSi, p.ShellBreakFeSi1, p.ShellBreakFeSi2};
     for (float v : vals)
         if (!std::isfinite(v)) return fail(GI_ERR_PARAMS, "pair table holds a non-finite value");
-    if (p.GMassFeFe < 0.0f || p.GMassSiSi < 0.0f || p.GMassFeSi < 0.0f)
-        return fail(GI_ERR_PARAMS, "negative G*m*m in the pair table");
+    if (!(p.GMassFeFe > 0.0f) || !(p.GMassSiSi > 0.0f) || !(p.GMassFeSi > 0.0f))
+        return fail(GI_ERR_PARAMS, "G*m*m must be positive for every pair class");
     // The far-field loop factorises G m_i m_j = gm_i gm_j.
     const double gfe = std::sqrt((double)p.GMassFeFe), gsi = std::sqrt((double)p.GMassSiSi);
     const double cross = gfe * gsi, want = (double)p.GMassFeSi;
@@ -144,6 +148,16 @@ static int to_device_params(const gi_pair_params &p, PairDev &d)
     d.Tmid[0] = d.Tband[0];
     d.Tmid[1] = r2_threshold(p.ShellBreakFeSi2);
     d.Tmid[2] = d.Tband[2];
+    // Contact corrections are summed in 64-bit fixed point: one pair's
+    // correction is at most |G - K (1 - r2)| + G m m <= 2 Gmax + Kmax, which
+    // maps to 2^40 units, leaving room for 2^22 contacts per body.
+    double gmax = 0.0, kmax = 0.0;
+    for (int t = 0; t < 3; ++t) {
+        gmax = std::max(gmax, (double)std::fabs(d.G[t]));
+        kmax = std::max({kmax, (double)std::fabs(d.K[t]), (double)std::fabs(d.KRmid[t]),
+                         (double)std::fabs(d.KRin[t])});
+    }
+    d.fx_unit = std::ldexp(2.0 * gmax + kmax, -40);
     return GI_OK;
 }
 
@@ -219,28 +233,39 @@ struct DeviceGuard {
     }
 };
 
+// Scratch owned per stream, so that launches on different streams of one
+// context never share a work queue, tickets or partial sums.
+struct StreamScratch {
+    unsigned int *tickets = nullptr;  // per i-block split tickets (zero between launches)
+    size_t tickets_cap = 0;
+    double *partials = nullptr;       // split-j partial sums
+    size_t partials_cap = 0;          // doubles
+    unsigned int *queue = nullptr;    // persistent-kernel work queue (2 counters)
+    float4 *pp_pos = nullptr, *pp_vel = nullptr;  // second state buffer of gi_step
+    size_t pp_cap = 0;                // bodies
+    unsigned int *grid_work = nullptr;  // cell grid of the contact pass (gi_grid.cu)
+    size_t grid_work_cap = 0;           // words
+    long long *delta = nullptr;         // contact corrections, 3 per body
+    size_t delta_cap = 0;               // bodies
+};
+
 struct gi_ctx {
     int device = 0;
     int sm_count = 0;
     gi_options opt{GI_SEP_REF_INT, GI_ACCUM_KAHAN};
     bool forced = false;
     gi_tuning forced_tuning{0, 0};
-    // Tuned decomposition per N bucket (floor(log2 n)): i-bodies per thread
-    // and the number of work items a run is split into.
+    // Tuned i-bodies per thread per N bucket (floor(log2 n)); 0 = default.
     int bucket_ipt[32] = {0};
-    int bucket_items[32] = {0};
-    unsigned int *tickets = nullptr;
-    size_t tickets_cap = 0;
-    double *partials = nullptr;
-    size_t partials_cap = 0;  // doubles
-    float4 *pp_pos = nullptr, *pp_vel = nullptr;
-    size_t pp_cap = 0;  // bodies
+    int bucket_shift[32] = {0};  // big-chunk size scale 2^shift of the default
+    std::map<cudaStream_t, StreamScratch> scratch;
     float4 *mirror_pos = nullptr, *mirror_vel = nullptr;
     size_t mirror_cap = 0;
     double *diag_work = nullptr;  // 16 doubles per block + 16 for the result
     int diag_blocks = 0;
     double *pot_buf = nullptr;
     size_t pot_cap = 0;
+    int occ[3][9];  // resident force CTAs per SM: [accum][i-bodies per thread]
 };
 
 static int ctx_init(gi_ctx *c, int device)
@@ -256,16 +281,30 @@ static int ctx_init(gi_ctx *c, int device)
                     device, prop.major, prop.minor);
     c->sm_count = prop.multiProcessorCount;
     c->diag_blocks = 2 * c->sm_count;
+    DeviceGuard g(device);
+    for (int acc = 0; acc < 3; ++acc)
+        for (int p : {1, 2, 4, 8}) {
+            const int o = std::min(gi_force_occupancy(p, acc, GI_EPI_FORCE),
+                                   gi_force_occupancy(p, acc, GI_EPI_STEP));
+            c->occ[acc][p] = std::max(o, 1);
+        }
     return GI_OK;
 }
 
 static void ctx_free(gi_ctx *c)
 {
     DeviceGuard g(c->device);
-    cudaFree(c->tickets);
-    cudaFree(c->partials);
-    cudaFree(c->pp_pos);
-    cudaFree(c->pp_vel);
+    for (auto &kv : c->scratch) {
+        StreamScratch &x = kv.second;
+        cudaFree(x.tickets);
+        cudaFree(x.partials);
+        cudaFree(x.queue);
+        cudaFree(x.pp_pos);
+        cudaFree(x.pp_vel);
+        cudaFree(x.grid_work);
+        cudaFree(x.delta);
+    }
+    c->scratch.clear();
     cudaFree(c->mirror_pos);
     cudaFree(c->mirror_vel);
     cudaFree(c->diag_work);
@@ -310,10 +349,13 @@ extern "C" int gi_ctx_set_tuning(gi_ctx *c, const gi_tuning *t)
 {
     if (!c) return fail(GI_ERR_INVALID_ARG, "ctx is NULL");
     if (!t) { c->forced = false; return GI_OK; }
-    if (t->i_per_thread != 1 && t->i_per_thread != 2 && t->i_per_thread != 4)
-        return fail(GI_ERR_INVALID_ARG, "i_per_thread must be 1, 2 or 4");
-    if (t->jchunk < 0 || t->jchunk % GI_NT != 0)
-        return fail(GI_ERR_INVALID_ARG, "jchunk must be a non-negative multiple of %d", GI_NT);
+    if (t->i_per_thread != 1 && t->i_per_thread != 2 && t->i_per_thread != 4 &&
+        t->i_per_thread != 8)
+        return fail(GI_ERR_INVALID_ARG, "i_per_thread must be 1, 2, 4 or 8");
+    if (t->jchunk < 0 || t->jchunk % GI_NT != 0 ||
+        (t->jchunk > 0 && (t->jchunk / GI_NT & (t->jchunk / GI_NT - 1)) != 0))
+        return fail(GI_ERR_INVALID_ARG,
+                    "jchunk must be 0 or %d times a power of two", GI_NT);
     c->forced = true;
     c->forced_tuning = *t;
     return GI_OK;
@@ -339,19 +381,47 @@ static void tuning_for(const gi_ctx *c, int n, int *ipt, int *jchunk)
     }
     const int b = bucket_of(std::max(n, 1));
     int p = c->bucket_ipt[b];
-    int items = c->bucket_items[b];
-    if (p == 0) {
-        p = n >= 32768 ? 4 : (n >= 8192 ? 2 : 1);
-        items = 16 * c->sm_count;
-    }
-    const int ib = GI_NT * p;
-    const int nib = (n + ib - 1) / ib;
-    int nsplit = std::max(1, (items + nib - 1) / std::max(nib, 1));
-    nsplit = std::min(nsplit, std::max(1, n / 1024));
-    int jc = (n + nsplit - 1) / nsplit;
-    jc = ((jc + GI_NT - 1) / GI_NT) * GI_NT;
+    if (p == 0) p = n >= 262144 ? 2 : 1;
+    // Big-chunk size (a power of two of tiles): a big item must be no longer
+    // than a quarter of one resident CTA's share of the run, so that the
+    // CTAs still have small items to even out their finishing times:
+    //   C (tiles) <= 1/4 * T * nib / slots, scaled by the tuned 2^shift.
+    // Depends on n and the context's tuning table only, so a run
+    // decomposes the same way alone and in any batch.
+    const int slots = c->sm_count * c->occ[c->opt.accum][p];
+    const int T = (n + GI_NT - 1) / GI_NT;
+    const int nib = (n + GI_NT * p - 1) / (GI_NT * p);
+    long long ct = std::max(1LL, (long long)T * nib / (4LL * slots));
+    const int shift = c->bucket_shift[b];
+    ct = shift >= 0 ? (ct << shift) : std::max(1LL, ct >> (-shift));
+    int lg = 0;
+    while ((2LL << lg) <= ct && (2LL << lg) <= T) ++lg;
     *ipt = p;
-    *jchunk = std::max(jc, GI_NT);
+    *jchunk = GI_NT << lg;
+}
+
+// Chunking of one run: chunks of 2^lg tiles, the last lg shrinking by
+// halves to one tile (see tail_tiles in gi_force_impl.cuh).
+static void chunking(int n, int jchunk, int *lg, int *tiles, int *nsplit)
+{
+    const int T = (n + GI_NT - 1) / GI_NT;
+    int l = 0;
+    while ((GI_NT << (l + 1)) <= jchunk) ++l;
+    if ((1LL << l) >= T) {  // one chunk holds the run
+        *lg = l;
+        *tiles = T;
+        *nsplit = 1;
+        return;
+    }
+    int r = 0;
+    long long covered = 0;
+    while (covered < T) {
+        covered = (r + 1 <= l) ? (1LL << (r + 1)) - 1 : (1LL << l) - 1 + (long long)(r + 1 - l) * (1LL << l);
+        ++r;
+    }
+    *lg = l;
+    *tiles = T;
+    *nsplit = r;
 }
 
 extern "C" int gi_ctx_get_tuning(gi_ctx *c, int n, gi_tuning *out)
@@ -367,6 +437,7 @@ extern "C" int gi_ctx_get_tuning(gi_ctx *c, int n, gi_tuning *out)
 struct Plan {
     std::vector<LaunchTable> tables;
     std::vector<int> ipt;
+    std::vector<long long> bodies;  // bodies in each table's runs
     size_t tickets = 0;   // max over tables (tables run one after another)
     size_t partials = 0;  // doubles, max over tables
     int max_end = 0;      // largest offset + n
@@ -424,7 +495,7 @@ static int make_plan(const gi_ctx *c, const gi_run *runs, int nruns,
         std::memset(&t, 0, sizeof t);
         t.sep_test = c->opt.sep_test;
         const int p = ipt[order[k]];
-        long long items = 0, tick = 0, part = 0;
+        long long items = 0, tick = 0, part = 0, nb = 0;
         while (k < order.size() && ipt[order[k]] == p && t.nruns < GI_MAX_RUNS) {
             const gi_run &q = runs[order[k]];
             RunDev &d = t.runs[t.nruns++];
@@ -433,11 +504,12 @@ static int make_plan(const gi_ctx *c, const gi_run *runs, int nruns,
             d.nfe = q.nfe;
             d.param = q.params;
             d.jchunk = jc[order[k]];
-            d.nsplit = (q.n + d.jchunk - 1) / d.jchunk;
+            chunking(q.n, d.jchunk, &d.lg, &d.tiles, &d.nsplit);
             d.nib = (q.n + GI_NT * p - 1) / (GI_NT * p);
             d.ipt = p;
             d.item_start = (int)items;
             items += (long long)d.nib * d.nsplit;
+            nb += q.n;
             if (d.nsplit > 1) {
                 d.tick_base = (int)tick;
                 d.part_base = part;
@@ -455,6 +527,7 @@ static int make_plan(const gi_ctx *c, const gi_run *runs, int nruns,
         for (size_t m = 0; m < pd.size(); ++m) t.params[m] = pd[m];
         plan.tables.push_back(t);
         plan.ipt.push_back(p);
+        plan.bodies.push_back(nb);
         plan.tickets = std::max(plan.tickets, (size_t)tick);
         plan.partials = std::max(plan.partials, (size_t)part);
     }
@@ -468,31 +541,55 @@ static bool stream_capturing(cudaStream_t s)
     return st != cudaStreamCaptureStatusNone;
 }
 
-static int ensure_scratch(gi_ctx *c, const Plan &plan, cudaStream_t s)
+static int ensure_scratch(gi_ctx *c, const Plan &plan, cudaStream_t s, StreamScratch **out)
 {
-    const bool grow_t = plan.tickets > c->tickets_cap;
-    const bool grow_p = plan.partials > c->partials_cap;
-    if (!grow_t && !grow_p) return GI_OK;
+    StreamScratch &x = c->scratch[s];
+    *out = &x;
+    const bool grow_t = plan.tickets > x.tickets_cap;
+    const bool grow_p = plan.partials > x.partials_cap;
+    size_t gwords = 0;
+    for (long long b : plan.bodies) gwords = std::max(gwords, gi_grid_words(plan.max_end, b));
+    const bool grow_g = gwords > x.grid_work_cap;
+    const bool grow_d = (size_t)plan.max_end > x.delta_cap;
+    if (!grow_t && !grow_p && !grow_g && !grow_d && x.queue) return GI_OK;
     if (stream_capturing(s))
         return fail(GI_ERR_INVALID_ARG,
                     "scratch must grow (run once outside stream capture before capturing)");
     GI_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    if (!x.queue) {
+        GI_CUDA(cudaMalloc(&x.queue, 2 * sizeof(unsigned int)), "cudaMalloc queue");
+        GI_CUDA(cudaMemset(x.queue, 0, 2 * sizeof(unsigned int)), "cudaMemset queue");
+    }
     if (grow_t) {
-        cudaFree(c->tickets);
-        c->tickets = nullptr;
-        c->tickets_cap = 0;
+        cudaFree(x.tickets);
+        x.tickets = nullptr;
+        x.tickets_cap = 0;
         size_t cap = std::max(plan.tickets, (size_t)1024);
-        GI_CUDA(cudaMalloc(&c->tickets, cap * sizeof(unsigned int)), "cudaMalloc tickets");
-        GI_CUDA(cudaMemset(c->tickets, 0, cap * sizeof(unsigned int)), "cudaMemset tickets");
-        c->tickets_cap = cap;
+        GI_CUDA(cudaMalloc(&x.tickets, cap * sizeof(unsigned int)), "cudaMalloc tickets");
+        GI_CUDA(cudaMemset(x.tickets, 0, cap * sizeof(unsigned int)), "cudaMemset tickets");
+        x.tickets_cap = cap;
     }
     if (grow_p) {
-        cudaFree(c->partials);
-        c->partials = nullptr;
-        c->partials_cap = 0;
+        cudaFree(x.partials);
+        x.partials = nullptr;
+        x.partials_cap = 0;
         size_t cap = plan.partials + plan.partials / 4;
-        GI_CUDA(cudaMalloc(&c->partials, cap * sizeof(double)), "cudaMalloc partials");
-        c->partials_cap = cap;
+        GI_CUDA(cudaMalloc(&x.partials, cap * sizeof(double)), "cudaMalloc partials");
+        x.partials_cap = cap;
+    }
+    if (grow_g) {
+        cudaFree(x.grid_work);
+        x.grid_work = nullptr;
+        x.grid_work_cap = 0;
+        GI_CUDA(cudaMalloc(&x.grid_work, gwords * sizeof(unsigned int)), "cudaMalloc grid");
+        x.grid_work_cap = gwords;
+    }
+    if (grow_d) {
+        cudaFree(x.delta);
+        x.delta = nullptr;
+        x.delta_cap = 0;
+        GI_CUDA(cudaMalloc(&x.delta, (size_t)plan.max_end * 3 * sizeof(long long)), "cudaMalloc delta");
+        x.delta_cap = plan.max_end;
     }
     return GI_OK;
 }
@@ -510,9 +607,9 @@ static int convert_params(const gi_pair_params *params, int nparams, std::vector
     return GI_OK;
 }
 
-static int run_force_plan(gi_ctx *c, const Plan &plan, int epi, const float4 *pos,
-                          const float4 *vel, float4 *force, float4 *pos_out,
-                          float4 *vel_out, cudaStream_t s)
+static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, int epi,
+                          const float4 *pos, const float4 *vel, float4 *force,
+                          float4 *pos_out, float4 *vel_out, cudaStream_t s)
 {
     for (size_t t = 0; t < plan.tables.size(); ++t) {
         ForceArgs a;
@@ -521,9 +618,17 @@ static int run_force_plan(gi_ctx *c, const Plan &plan, int epi, const float4 *po
         a.force = force;
         a.pos_out = pos_out;
         a.vel_out = vel_out;
-        a.partials = c->partials;
-        a.tickets = c->tickets;
-        GI_CUDA(gi_launch_force(plan.ipt[t], c->opt.accum, epi, a, plan.tables[t], s),
+        a.partials = x->partials;
+        a.tickets = x->tickets;
+        a.queue = x->queue;
+        a.delta = x->delta;
+        // contact pass first: the force epilogue adds its corrections
+        GI_CUDA(gi_launch_contacts(pos, vel, plan.tables[t], plan.bodies[t], plan.max_end,
+                                   x->grid_work, x->delta, c->sm_count, s),
+                "contact pass");
+        const int p = plan.ipt[t];
+        const int grid = c->sm_count * c->occ[c->opt.accum][p];
+        GI_CUDA(gi_launch_force(p, c->opt.accum, epi, a, plan.tables[t], grid, s),
                 "force kernel launch");
     }
     return GI_OK;
@@ -548,8 +653,9 @@ extern "C" int gi_forces(gi_ctx *c, const float *pos, const float *vel, float *f
         return st;
     DeviceGuard g(c->device);
     cudaStream_t s = (cudaStream_t)stream;
-    if ((st = ensure_scratch(c, plan, s))) return st;
-    return run_force_plan(c, plan, GI_EPI_FORCE, (const float4 *)pos, (const float4 *)vel,
+    StreamScratch *x = nullptr;
+    if ((st = ensure_scratch(c, plan, s, &x))) return st;
+    return run_force_plan(c, x, plan, GI_EPI_FORCE, (const float4 *)pos, (const float4 *)vel,
                           (float4 *)force, nullptr, nullptr, s);
 }
 
@@ -603,20 +709,20 @@ extern "C" int gi_move(gi_ctx *c, float *pos, float *vel, const float *force,
     return move_impl(pos, vel, force, runs, nruns, (cudaStream_t)stream);
 }
 
-static int ensure_pingpong(gi_ctx *c, size_t bodies, cudaStream_t s)
+static int ensure_pingpong(StreamScratch *x, size_t bodies, cudaStream_t s)
 {
-    if (bodies <= c->pp_cap) return GI_OK;
+    if (bodies <= x->pp_cap) return GI_OK;
     if (stream_capturing(s))
         return fail(GI_ERR_INVALID_ARG,
                     "state buffers must grow (run once outside stream capture before capturing)");
     GI_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-    cudaFree(c->pp_pos);
-    cudaFree(c->pp_vel);
-    c->pp_pos = c->pp_vel = nullptr;
-    c->pp_cap = 0;
-    GI_CUDA(cudaMalloc(&c->pp_pos, bodies * sizeof(float4)), "cudaMalloc state");
-    GI_CUDA(cudaMalloc(&c->pp_vel, bodies * sizeof(float4)), "cudaMalloc state");
-    c->pp_cap = bodies;
+    cudaFree(x->pp_pos);
+    cudaFree(x->pp_vel);
+    x->pp_pos = x->pp_vel = nullptr;
+    x->pp_cap = 0;
+    GI_CUDA(cudaMalloc(&x->pp_pos, bodies * sizeof(float4)), "cudaMalloc state");
+    GI_CUDA(cudaMalloc(&x->pp_vel, bodies * sizeof(float4)), "cudaMalloc state");
+    x->pp_cap = bodies;
     return GI_OK;
 }
 
@@ -635,11 +741,12 @@ extern "C" int gi_step(gi_ctx *c, float *pos, float *vel, const gi_run *runs, in
     if ((st = check_body_ptr(pos, "pos")) || (st = check_body_ptr(vel, "vel"))) return st;
     DeviceGuard g(c->device);
     cudaStream_t s = (cudaStream_t)stream;
-    if ((st = ensure_scratch(c, plan, s))) return st;
-    if ((st = ensure_pingpong(c, (size_t)plan.max_end, s))) return st;
-    float4 *ip = (float4 *)pos, *iv = (float4 *)vel, *op = c->pp_pos, *ov = c->pp_vel;
+    StreamScratch *x = nullptr;
+    if ((st = ensure_scratch(c, plan, s, &x))) return st;
+    if ((st = ensure_pingpong(x, (size_t)plan.max_end, s))) return st;
+    float4 *ip = (float4 *)pos, *iv = (float4 *)vel, *op = x->pp_pos, *ov = x->pp_vel;
     for (int k = 0; k < nsteps; ++k) {
-        if ((st = run_force_plan(c, plan, GI_EPI_STEP, ip, iv, nullptr, op, ov, s))) return st;
+        if ((st = run_force_plan(c, x, plan, GI_EPI_STEP, ip, iv, nullptr, op, ov, s))) return st;
         std::swap(ip, op);
         std::swap(iv, ov);
     }
@@ -654,6 +761,111 @@ extern "C" int gi_step(gi_ctx *c, float *pos, float *vel, const gi_run *runs, in
         }
     }
     return GI_OK;
+}
+
+extern "C" int gi_step_pingpong(gi_ctx *c, float *pos_a, float *vel_a, float *pos_b,
+                                float *vel_b, const gi_run *runs, int nruns,
+                                const gi_pair_params *params, int nparams, int nsteps,
+                                void *stream)
+{
+    if (!c) return fail(GI_ERR_INVALID_ARG, "ctx is NULL");
+    if (nsteps < 0) return fail(GI_ERR_INVALID_ARG, "nsteps = %d", nsteps);
+    int st = check_runs(runs, nruns, nparams);
+    if (st) return st;
+    std::vector<PairDev> pd;
+    if ((st = convert_params(params, nparams, pd))) return st;
+    Plan plan;
+    if ((st = make_plan(c, runs, nruns, pd, plan))) return st;
+    if (plan.tables.empty() || nsteps == 0) return GI_OK;
+    if ((st = check_body_ptr(pos_a, "pos_a")) || (st = check_body_ptr(vel_a, "vel_a")) ||
+        (st = check_body_ptr(pos_b, "pos_b")) || (st = check_body_ptr(vel_b, "vel_b")))
+        return st;
+    if (pos_a == pos_b || vel_a == vel_b)
+        return fail(GI_ERR_INVALID_ARG, "the two state buffers must differ");
+    DeviceGuard g(c->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    StreamScratch *x = nullptr;
+    if ((st = ensure_scratch(c, plan, s, &x))) return st;
+    float4 *ip = (float4 *)pos_a, *iv = (float4 *)vel_a, *op = (float4 *)pos_b,
+           *ov = (float4 *)vel_b;
+    for (int k = 0; k < nsteps; ++k) {
+        if ((st = run_force_plan(c, x, plan, GI_EPI_STEP, ip, iv, nullptr, op, ov, s))) return st;
+        std::swap(ip, op);
+        std::swap(iv, ov);
+    }
+    return GI_OK;
+}
+
+// Autotuner: for each N bucket present in `runs` (its largest run stands for
+// it), time the force pass for every i-bodies-per-thread value and big-chunk
+// scale, on the caller's own bodies, and keep the fastest in the context's
+// table.  Synchronous; allocates a scratch force array for the timing.
+extern "C" int gi_autotune(gi_ctx *c, const float *pos, const float *vel, const gi_run *runs,
+                           int nruns, const gi_pair_params *params, int nparams, void *stream)
+{
+    if (!c) return fail(GI_ERR_INVALID_ARG, "ctx is NULL");
+    int st = check_runs(runs, nruns, nparams);
+    if (st) return st;
+    if (stream_capturing((cudaStream_t)stream))
+        return fail(GI_ERR_INVALID_ARG, "gi_autotune cannot run under stream capture");
+    DeviceGuard g(c->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    int rep[32];
+    for (int b = 0; b < 32; ++b) rep[b] = -1;
+    int max_end = 0;
+    for (int r = 0; r < nruns; ++r) {
+        if (runs[r].n <= 0) continue;
+        const int b = bucket_of(runs[r].n);
+        if (rep[b] < 0 || runs[r].n > runs[rep[b]].n) rep[b] = r;
+        max_end = std::max(max_end, runs[r].offset + runs[r].n);
+    }
+    if (max_end == 0) return GI_OK;
+    const bool was_forced = c->forced;
+    c->forced = false;
+    float *force = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t ce = cudaMalloc(&force, (size_t)max_end * sizeof(float4));
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaFree(force);
+        c->forced = was_forced;
+        return cuda_fail(ce, "autotune setup");
+    }
+    for (int b = 0; b < 32 && st == GI_OK; ++b) {
+        if (rep[b] < 0) continue;
+        const gi_run &q = runs[rep[b]];
+        const bool big = q.n > 262144;
+        const int ipts[3] = {1, 2, 4};
+        float best = 1e30f;
+        int best_p = 1, best_s = 0;
+        for (int pi = 0; pi < (big ? 2 : 3) && st == GI_OK; ++pi) {
+            for (int sh = (big ? -1 : -2); sh <= (big ? 1 : 2) && st == GI_OK; ++sh) {
+                c->bucket_ipt[b] = ipts[pi];
+                c->bucket_shift[b] = sh;
+                // warm-up (also grows scratch), then two timed passes
+                st = gi_forces(c, pos, vel, force, &q, 1, params, nparams, stream);
+                if (st) break;
+                cudaEventRecord(e0, s);
+                for (int rep2 = 0; rep2 < 2 && st == GI_OK; ++rep2)
+                    st = gi_forces(c, pos, vel, force, &q, 1, params, nparams, stream);
+                cudaEventRecord(e1, s);
+                if (st) break;
+                ce = cudaEventSynchronize(e1);
+                if (ce != cudaSuccess) { st = cuda_fail(ce, "autotune timing"); break; }
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best) { best = ms; best_p = ipts[pi]; best_s = sh; }
+            }
+        }
+        c->bucket_ipt[b] = best_p;
+        c->bucket_shift[b] = best_s;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(force);
+    c->forced = was_forced;
+    return st;
 }
 
 extern "C" int gi_run_host(gi_ctx *c, float *pos_host, float *vel_host, int ntotal,

@@ -28,6 +28,7 @@
 // Pair constants indexed by the pair class test = (i is Fe) + (j is Fe):
 // 0 = Si-Si, 1 = Fe-Si, 2 = Fe-Fe.
 struct PairDev {
+    double fx_unit;      // fixed-point unit of the contact corrections (force)
     float gm_fe, gm_si;  // sqrt(G) m: G m_i m_j = gm_i gm_j (far-field gravity)
     float G[3];          // G m_i m_j of the class (contact band)
     float K[3];          // full stiffness
@@ -41,8 +42,10 @@ struct RunDev {
     int offset, n, nfe, param;
     int item_start;   // first work item of this run
     int nsplit;       // j-chunks per i-block
-    int jchunk;       // bodies per j-chunk (multiple of GI_NT)
+    int jchunk;       // bodies per big chunk (GI_NT * 2^lg)
     int nib;          // i-blocks
+    int lg;           // log2 of the big chunk in tiles of GI_NT bodies
+    int tiles;        // tiles of the run, ceil(n / GI_NT)
     int tick_base;    // first ticket of this run
     long long part_base;  // first double of this run's partial sums
     float dt, dtm_fe, dtm_si, damp;
@@ -66,16 +69,27 @@ struct ForceArgs {
     float4 *vel_out;   // GI_EPI_STEP
     double *partials;  // split-j partial sums (nullptr when no run splits)
     unsigned int *tickets;
+    unsigned int *queue;  // [0] next work item, [1] CTAs finished (zero between launches)
+    const long long *delta;  // contact corrections, 3 per body, fixed point (gi_grid.cu)
 };
 
 // Launchers (gi_force_ipt*.cu).  Return cudaError_t of the launch.
 cudaError_t gi_launch_force(int ipt, int acc, int epi, const ForceArgs &a,
-                            const LaunchTable &tab, cudaStream_t s);
-cudaError_t gi_launch_force_ipt1(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, cudaStream_t s);
-cudaError_t gi_launch_force_ipt2(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, cudaStream_t s);
-cudaError_t gi_launch_force_ipt4(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, cudaStream_t s);
+                            const LaunchTable &tab, int grid, cudaStream_t s);
+cudaError_t gi_launch_force_ipt1(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, int grid, cudaStream_t s);
+cudaError_t gi_launch_force_ipt2(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, int grid, cudaStream_t s);
+cudaError_t gi_launch_force_ipt4(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, int grid, cudaStream_t s);
+cudaError_t gi_launch_force_ipt8(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, int grid, cudaStream_t s);
 // Resident CTAs per SM of a force kernel instance (for the planner).
 int gi_force_occupancy(int ipt, int acc, int epi);
+
+// gi_grid.cu: contact corrections of every body of the table's runs into
+// delta (3 x int64 per body) through a hashed cell grid.
+unsigned int gi_grid_buckets(long long bodies);
+size_t gi_grid_words(long long max_end, long long bodies);
+cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const LaunchTable &tab,
+                               long long bodies, int max_end, unsigned int *work,
+                               long long *delta, int nsm, cudaStream_t s);
 
 // gi_aux.cu
 cudaError_t gi_launch_move(float4 *pos, float4 *vel, const float4 *force,

@@ -96,9 +96,13 @@ _SIGS = {
     "gi_ctx_get_tuning": ([_P, C.c_int, C.POINTER(Tuning)], C.c_int),
     "gi_forces": ([_P, _P, _P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams), C.c_int, _P],
                   C.c_int),
+    "gi_autotune": ([_P, _P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams), C.c_int, _P],
+                    C.c_int),
     "gi_move": ([_P, _P, _P, _P, C.POINTER(Run), C.c_int, _P], C.c_int),
     "gi_step": ([_P, _P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams), C.c_int, C.c_int,
                  _P], C.c_int),
+    "gi_step_pingpong": ([_P, _P, _P, _P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams),
+                          C.c_int, C.c_int, _P], C.c_int),
     "gi_diag_fp64": ([_P, _P, _P, _P, C.c_int, C.POINTER(Run), C.POINTER(PairParams),
                       C.POINTER(C.c_double), _P], C.c_int),
     "gi_potential_fp64": ([_P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams), C.c_int,
@@ -250,6 +254,11 @@ class Context:
         check(lib().gi_ctx_get_tuning(self.h, n, C.byref(t)))
         return t.i_per_thread, t.jchunk
 
+    def autotune(self, pos, vel, runs, params, stream=0):
+        ra, nr = _arr(runs, Run)
+        pa, npar = _arr(params, PairParams)
+        check(lib().gi_autotune(self.h, pos, vel, ra, nr, pa, npar, stream))
+
     def forces(self, pos, vel, force, runs, params, stream=0):
         ra, nr = _arr(runs, Run)
         pa, npar = _arr(params, PairParams)
@@ -263,6 +272,12 @@ class Context:
         ra, nr = _arr(runs, Run)
         pa, npar = _arr(params, PairParams)
         check(lib().gi_step(self.h, pos, vel, ra, nr, pa, npar, nsteps, stream))
+
+    def step_pingpong(self, pos_a, vel_a, pos_b, vel_b, runs, params, nsteps, stream=0):
+        ra, nr = _arr(runs, Run)
+        pa, npar = _arr(params, PairParams)
+        check(lib().gi_step_pingpong(self.h, pos_a, vel_a, pos_b, vel_b, ra, nr, pa, npar, nsteps,
+                                     stream))
 
     def diag(self, pos, vel, run, params, label=None, scope=0, stream=0) -> list[float]:
         out = (C.c_double * 15)()

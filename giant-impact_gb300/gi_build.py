@@ -25,7 +25,8 @@ INCLUDE = os.path.join(ROOT, "include")
 ORACLE = os.path.join(ROOT, "oracle")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["gi_force_ipt1.cu", "gi_force_ipt2.cu", "gi_force_ipt4.cu", "gi_aux.cu", "gi_api.cu"]
+CU_SOURCES = ["gi_force_ipt1.cu", "gi_force_ipt2.cu", "gi_force_ipt4.cu", "gi_force_ipt8.cu",
+              "gi_grid.cu", "gi_aux.cu", "gi_api.cu"]
 CPP_SOURCES = ["gi_host.cpp"]
 
 

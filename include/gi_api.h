@@ -120,8 +120,8 @@ typedef struct gi_move_separate_consts {
  * reduced stiffness of a separating pair inside its shell, ShellBreak* =
  * D (1 - SD) (impactAddTime.cu:128-170).  MassFe / MassSi are the element
  * masses (used by the FP64 diagnostics).  The gravity table must be
- * rank one: GMassFeSi^2 == GMassFeFe * GMassSiSi (true whenever it comes
- * from G, mFe, mSi). */
+ * positive and rank one: GMassFeSi^2 == GMassFeFe * GMassSiSi (true
+ * whenever it comes from G > 0, mFe, mSi). */
 typedef struct gi_pair_params {
     float GMassFeFe, GMassFeSi, GMassSiSi;
     float KFeFe, KSiSi, KFeSi;
@@ -150,7 +150,7 @@ typedef struct gi_run {
 
 /* Per-body force accumulation. */
 #define GI_ACCUM_KAHAN 0   /* FP32 per j-tile, Kahan-compensated across tiles */
-#define GI_ACCUM_FP32 1    /* plain FP32                                      */
+#define GI_ACCUM_FP32 1    /* FP32 per j-tile, plain FP32 across tiles        */
 #define GI_ACCUM_FP64 2    /* FP32 per j-tile, FP64 across tiles              */
 
 typedef struct gi_options {
@@ -159,9 +159,10 @@ typedef struct gi_options {
 } gi_options;
 
 /* Work decomposition of one run (chosen per N bucket by the autotuner or
- * set explicitly).  i_per_thread in {1, 2, 4}; jchunk a multiple of 128
- * (0 = whole run in one chunk).  The result for a run depends only on
- * these two numbers, never on what else is in the batch. */
+ * set explicitly).  i_per_thread in {1, 2, 4, 8}; jchunk = 128 * 2^k bodies
+ * per big j-chunk (the last chunks shrink by halves to 128 bodies), or 0 =
+ * the whole run in one chunk.  The result for a run depends only on these
+ * two numbers, never on what else is in the batch. */
 typedef struct gi_tuning {
     int i_per_thread;
     int jchunk;
@@ -225,6 +226,14 @@ int gi_ctx_set_tuning(gi_ctx *ctx, const gi_tuning *tuning);
 /* The decomposition the context would use for a run of n bodies. */
 int gi_ctx_get_tuning(gi_ctx *ctx, int n, gi_tuning *out);
 
+/* Autotuner: for each N bucket (floor(log2 n)) among `runs`, times the
+ * force pass for i_per_thread in {1, 2, 4} and five big-chunk sizes on the
+ * caller's own bodies, and stores the fastest in the context (synchronous;
+ * allocates a temporary force array).  Later calls decompose runs of those
+ * buckets with the tuned values; results depend only on n and this table. */
+int gi_autotune(gi_ctx *ctx, const float *pos, const float *vel, const gi_run *runs,
+                int nruns, const gi_pair_params *params, int nparams, void *stream);
+
 /* Force pass over nruns independent runs (one launch): force[i].xyz for
  * every body of every run. */
 int gi_forces(gi_ctx *ctx, const float *pos, const float *vel, float *force,
@@ -242,6 +251,16 @@ int gi_move(gi_ctx *ctx, float *pos, float *vel, const float *force,
 int gi_step(gi_ctx *ctx, float *pos, float *vel, const gi_run *runs,
             int nruns, const gi_pair_params *params, int nparams, int nsteps,
             void *stream);
+
+/* nsteps fused steps alternating between two caller-owned state buffers
+ * (a -> b -> a ...): the state after an odd number of steps is in b, after
+ * an even number in a.  No copies, no library-owned state buffer: the
+ * building block of graph-captured step loops.  Same kernels and results as
+ * gi_step. */
+int gi_step_pingpong(gi_ctx *ctx, float *pos_a, float *vel_a, float *pos_b,
+                     float *vel_b, const gi_run *runs, int nruns,
+                     const gi_pair_params *params, int nparams, int nsteps,
+                     void *stream);
 
 /* FP64 diagnostics of one run (synchronous: returns with out filled).
  * label (device, one byte per body of the whole array, may be NULL)

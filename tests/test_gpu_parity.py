@@ -223,6 +223,44 @@ def test_fused_step_equals_force_then_move(gi, torch_cuda, ctx):
     assert torch.equal(dp, ep) and torch.equal(dv, ev)
 
 
+def test_pingpong_matches_in_place_step(gi, torch_cuda, ctx):
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    pos, vel, nfe = gi.ic_lattice(15, 7000, vel_sigma=1.0)
+    run = wl.run_desc(gi, 0, 7000, nfe)
+    a = (dev(torch, pos), dev(torch, vel))
+    b = (torch.zeros_like(a[0]), torch.zeros_like(a[1]))
+    ctx.step_pingpong(a[0].data_ptr(), a[1].data_ptr(), b[0].data_ptr(), b[1].data_ptr(), [run], p, 3)
+    c = (dev(torch, pos), dev(torch, vel))
+    ctx.step(c[0].data_ptr(), c[1].data_ptr(), [run], p, 3)
+    torch.cuda.synchronize()
+    assert torch.equal(b[0], c[0]) and torch.equal(b[1], c[1])  # odd step count ends in b
+    with pytest.raises(gi.GIError):
+        ctx.step_pingpong(a[0].data_ptr(), a[1].data_ptr(), a[0].data_ptr(), b[1].data_ptr(), [run], p, 1)
+
+
+def test_contacts_deterministic_and_bucket_independent(gi, torch_cuda):
+    """Contact corrections are summed in fixed point: repeated passes (whose
+    bucket order varies with the atomics) give bit-identical forces, also
+    for a dense clump where hundreds of bodies overlap."""
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    pos, vel, nfe = ball_with_velocities(gi, 30000, 19)
+    # a dense clump: 600 bodies squeezed into a ball of radius 2
+    rng = np.random.default_rng(3)
+    cl = rng.normal(size=(600, 3))
+    cl = cl / np.linalg.norm(cl, axis=1, keepdims=True) * rng.uniform(0, 2.0, size=(600, 1))
+    pos[:600, :3] = cl.astype(np.float32)
+    run = wl.run_desc(gi, 0, 30000, nfe)
+    c = gi.Context(0)
+    f1 = gpu_forces(gi, torch, c, pos, vel, [run], p)
+    f2 = gpu_forces(gi, torch, c, pos, vel, [run], p)
+    c.close()
+    assert np.array_equal(f1[:, :3], f2[:, :3])
+
+
 def test_batch_invariance(gi, torch_cuda, ctx):
     """A run's forces are bit-identical alone and inside a batch."""
     torch = torch_cuda
@@ -241,7 +279,7 @@ def test_batch_invariance(gi, torch_cuda, ctx):
         assert np.array_equal(alone[:, :3], mixed[o:o + s, :3]), k
 
 
-@pytest.mark.parametrize("ipt,jchunk", [(1, 0), (2, 1024), (4, 2048), (4, 128), (1, 384)])
+@pytest.mark.parametrize("ipt,jchunk", [(1, 0), (2, 1024), (4, 2048), (4, 128), (1, 512), (8, 256)])
 def test_decompositions_agree(gi, orc, torch_cuda, ctx, ipt, jchunk):
     p = config1_params(gi)
     pos, vel, nfe = gi.ic_lattice(9, 5000, vel_sigma=1.5)
@@ -269,6 +307,25 @@ def test_accumulation_modes(gi, orc, torch_cuda, accum):
     err = rel_l2(f[idx, :3], f64)
     print(f"accum {accum}: rel L2 {err:.3e}")
     assert err < (2e-5 if accum == 1 else FORCE_TOL)
+
+
+def test_autotune_keeps_results_within_tolerance(gi, orc, torch_cuda):
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    pos, vel, nfe = ball_with_velocities(gi, 20000, 23)
+    run = wl.run_desc(gi, 0, 20000, nfe)
+    c = gi.Context(0)
+    dp, dv = dev(torch, pos), dev(torch, vel)
+    c.autotune(dp.data_ptr(), dv.data_ptr(), [run], p)
+    tuned = c.get_tuning(20000)
+    f = gpu_forces(gi, torch, c, pos, vel, [run], p)
+    c.close()
+    idx = np.arange(0, 20000, 11)
+    f64, _ = orc.forces_fp64(pos, vel, [(0, 20000, nfe, 0, 0, 0, 0, 0)], p, idx=idx)
+    print("tuned", tuned)
+    assert tuned[0] in (1, 2, 4)
+    assert rel_l2(f[idx, :3], f64) < FORCE_TOL
 
 
 def test_sign_separation_mode(gi, orc, torch_cuda):
