@@ -1122,3 +1122,14 @@ extern "C" int gi_move_damped_separate(float *pos, float *vel, const float *forc
     r[1].damp = damp2;
     return move_impl(pos, vel, force, r, 2, (cudaStream_t)stream);
 }
+
+// ------------------------------------------------------ internal helpers --
+
+int gi_internal_fail(int status, const char *msg) { return fail(status, "%s", msg); }
+
+int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d)
+{
+    gi_pair_params p;
+    gi_params_from_collision_consts(c, &p);
+    return to_device_params(p, *d);
+}

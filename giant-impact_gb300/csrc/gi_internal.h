@@ -103,3 +103,9 @@ cudaError_t gi_launch_potential(const float4 *pos, const LaunchTable &tab,
                                 double *per_block, int nblocks_per_run,
                                 cudaStream_t s);
 cudaError_t gi_launch_ffma_peak(float *sink, int blocks, int iters, cudaStream_t s);
+
+// gi_api.cu helpers for the library's other translation units: record an
+// error for gi_last_error() and return `status`; the device pair table of a
+// reference collision struct.
+int gi_internal_fail(int status, const char *msg);
+int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d);

@@ -1,0 +1,175 @@
+// gi_noalloc.cu -- the collision force pass for callers that cannot allocate
+// device memory.
+//
+// gi_forces_collision, the regular drop-in, takes its scratch memory (work
+// queue, split tickets, partial sums, cell grid, contact corrections) from a
+// library context that grows it with cudaMalloc on first use.  Some callers
+// cannot let a library do that:
+//   - applications that hand out device memory only from their own budget or
+//     pool (a run admitted against a fixed HBM budget, a GPU shared under a
+//     per-process memory limit), where a hidden allocation could fail at an
+//     arbitrary step or silently break the budget;
+//   - latency-sensitive step loops that must not stall: cudaMalloc and
+//     cudaFree can synchronise the whole device, holding up every stream.
+// For them, gi_forces_collision_noalloc computes the same forces with all of
+// its scratch in one statically allocated device array, g_noalloc_scratch,
+// of GI_NOALLOC_BYTES (10 MiB).  Every GPU that loads the library holds that
+// array until the process exits.  The array limits a call to
+// GI_NOALLOC_MAX_BODIES (32,768) bodies; larger calls are refused.
+//
+// Every call shares the one array and leaves its contents behind: the
+// counters that must start at zero are cleared at the start of each call (in
+// stream order), everything else is fully written before it is read.  Calls
+// that overlap on the GPU (for example on two streams) race on the array and
+// corrupt each other's results; serialise them.
+//
+// Host code cannot use the array's name as a device address (on the host it
+// names a stand-in object).  The device address is obtained once per device
+// with cudaGetSymbolAddress, with that device current, by the first call on
+// that device; make that first call before any stream capture.
+#include <cstring>
+#include <mutex>
+
+#include "gi_internal.h"
+
+#define GI_NOALLOC_BYTES (10u << 20)
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GI_NOALLOC_BYTES];
+
+namespace {
+
+constexpr int kIpt = 2;    // i-bodies per thread
+constexpr int kLg = 6;     // big j-chunks of 2^6 tiles (8,192 bodies)
+constexpr int kMaxSplit = 10;  // j-chunks per i-block for n <= GI_NOALLOC_MAX_BODIES
+constexpr size_t kMaxBodies = GI_NOALLOC_MAX_BODIES;
+constexpr size_t kQueueOff = 0;      // 2 x uint32, then one ticket per i-block
+constexpr size_t kCountersBytes = 4096;
+constexpr size_t kDeltaOff = kCountersBytes;  // 3 x int64 per body
+constexpr size_t kGridOff = kDeltaOff + 3 * sizeof(long long) * kMaxBodies;
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+std::mutex g_mu;
+void *g_base[64] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device (set-up on the
+// first call per device).
+int scratch_base(void **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return gi_internal_fail(GI_ERR_CUDA, "cudaGetDevice failed");
+    if (dev < 0 || dev >= 64) return gi_internal_fail(GI_ERR_NO_DEVICE, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_base[dev]) {
+        void *ptr = nullptr;
+        e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return gi_internal_fail(GI_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed");
+        g_base[dev] = ptr;
+    }
+    *out = g_base[dev];
+    return GI_OK;
+}
+
+// Chunks per i-block for a run of T tiles with big chunks of 2^kLg tiles
+// (the layout the force kernel decodes, see tail_tiles).
+int nsplit_for(int T)
+{
+    if ((1 << kLg) >= T) return 1;
+    int r = 0;
+    long long covered = 0;
+    while (covered < T) {
+        covered = (r + 1 <= kLg) ? (1LL << (r + 1)) - 1
+                                 : (1LL << kLg) - 1 + (long long)(r + 1 - kLg) * (1LL << kLg);
+        ++r;
+    }
+    return r;
+}
+
+}  // namespace
+
+extern "C" int gi_forces_collision_noalloc(const float *pos, const float *vel, float *force,
+                                           const gi_force_collision_consts *cc, int n,
+                                           void *stream)
+{
+    if (!cc) return gi_internal_fail(GI_ERR_INVALID_ARG, "consts is NULL");
+    if (n < 0) return gi_internal_fail(GI_ERR_BAD_SIZE, "n is negative");
+    if ((size_t)n > kMaxBodies)
+        return gi_internal_fail(GI_ERR_BAD_SIZE,
+                                "gi_forces_collision_noalloc takes at most GI_NOALLOC_MAX_BODIES "
+                                "(32768) bodies; use gi_forces_collision for larger runs");
+    if (cc->NFe < 0) return gi_internal_fail(GI_ERR_BAD_SIZE, "NFe is negative");
+    if (n == 0) return GI_OK;
+    if (!pos || !vel || !force) return gi_internal_fail(GI_ERR_INVALID_ARG, "body array is NULL");
+    if ((reinterpret_cast<uintptr_t>(pos) | reinterpret_cast<uintptr_t>(vel) |
+         reinterpret_cast<uintptr_t>(force)) % 16 != 0)
+        return gi_internal_fail(GI_ERR_ALIGNMENT, "body arrays must be 16-byte aligned");
+
+    LaunchTable tab;
+    std::memset(&tab, 0, sizeof tab);
+    int st = gi_internal_collision_pairdev(cc, &tab.params[0]);
+    if (st) return st;
+    const int T = (n + GI_NT - 1) / GI_NT;
+    RunDev &d = tab.runs[0];
+    d.offset = 0;
+    d.n = n;
+    d.nfe = cc->NFe < n ? cc->NFe : n;
+    d.param = 0;
+    d.ipt = kIpt;
+    d.nib = (n + GI_NT * kIpt - 1) / (GI_NT * kIpt);
+    d.lg = kLg;
+    d.tiles = T;
+    d.jchunk = GI_NT << kLg;
+    d.nsplit = nsplit_for(T);
+    d.item_start = 0;
+    d.tick_base = 0;
+    d.part_base = 0;
+    tab.nruns = 1;
+    tab.nitems = d.nib * d.nsplit;
+    tab.sep_test = GI_SEP_REF_INT;
+
+    // Carve the static array.
+    const size_t grid_bytes = align256(gi_grid_words(n, n) * sizeof(unsigned int));
+    const size_t part_off = kGridOff + grid_bytes;
+    const size_t part_bytes = (size_t)kMaxSplit * 3 * sizeof(double) * kMaxBodies;
+    if (d.nsplit > kMaxSplit || part_off + part_bytes > GI_NOALLOC_BYTES ||
+        2 * sizeof(unsigned int) + (size_t)d.nib * sizeof(unsigned int) > kCountersBytes)
+        return gi_internal_fail(GI_ERR_BAD_SIZE, "static scratch layout does not fit this run");
+    void *base = nullptr;
+    if ((st = scratch_base(&base))) return st;
+    unsigned char *b = static_cast<unsigned char *>(base);
+    unsigned int *queue = reinterpret_cast<unsigned int *>(b + kQueueOff);
+    unsigned int *tickets = queue + 2;
+    long long *delta = reinterpret_cast<long long *>(b + kDeltaOff);
+    unsigned int *grid = reinterpret_cast<unsigned int *>(b + kGridOff);
+    double *partials = reinterpret_cast<double *>(b + part_off);
+
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return gi_internal_fail(GI_ERR_CUDA, "device query failed");
+    cudaStream_t s = (cudaStream_t)stream;
+    // The queue and tickets must start at zero; the array keeps whatever the
+    // previous call left, so clear them in stream order.
+    if (cudaMemsetAsync(b + kQueueOff, 0, kCountersBytes, s) != cudaSuccess)
+        return gi_internal_fail(GI_ERR_CUDA, "clearing the static scratch counters failed");
+    if (gi_launch_contacts(reinterpret_cast<const float4 *>(pos), reinterpret_cast<const float4 *>(vel),
+                           tab, n, n, grid, delta, nsm, s) != cudaSuccess)
+        return gi_internal_fail(GI_ERR_CUDA, "contact pass launch failed");
+    ForceArgs a;
+    a.pos = reinterpret_cast<const float4 *>(pos);
+    a.vel = reinterpret_cast<const float4 *>(vel);
+    a.force = reinterpret_cast<float4 *>(force);
+    a.pos_out = nullptr;
+    a.vel_out = nullptr;
+    a.partials = partials;
+    a.tickets = tickets;
+    a.queue = queue;
+    a.delta = delta;
+    int occ = gi_force_occupancy(kIpt, GI_ACC_KAHAN, GI_EPI_FORCE);
+    if (occ < 1) occ = 1;
+    if (gi_launch_force(kIpt, GI_ACC_KAHAN, GI_EPI_FORCE, a, tab, nsm * occ, s) != cudaSuccess)
+        return gi_internal_fail(GI_ERR_CUDA, "force kernel launch failed");
+    return GI_OK;
+}

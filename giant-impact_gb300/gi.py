@@ -85,6 +85,8 @@ _SIGS = {
     "gi_device_info": ([C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                         C.POINTER(C.c_longlong)], C.c_int),
     "gi_forces_collision": ([_P, _P, _P, C.POINTER(ForceCollisionConsts), C.c_int, _P], C.c_int),
+    "gi_forces_collision_noalloc": ([_P, _P, _P, C.POINTER(ForceCollisionConsts), C.c_int, _P],
+                                    C.c_int),
     "gi_move_collision": ([_P, _P, _P, C.POINTER(MoveCollisionConsts), C.c_int, _P], C.c_int),
     "gi_forces_separate": ([_P, _P, _P, C.POINTER(ForceSeparateConsts), C.c_int, _P], C.c_int),
     "gi_move_damped_separate": ([_P, _P, _P, C.POINTER(MoveSeparateConsts), C.c_float,
@@ -203,6 +205,15 @@ def measure_ffma_peak(device: int = 0) -> float:
 
 def forces_collision(pos, vel, force, consts, n, stream=0):
     check(lib().gi_forces_collision(pos, vel, force, C.byref(consts), n, stream))
+
+
+def forces_collision_noalloc(pos, vel, force, consts, n, stream=0):
+    """gi_forces_collision without any device allocation (static scratch,
+    n <= NOALLOC_MAX_BODIES; calls must not overlap on the GPU)."""
+    check(lib().gi_forces_collision_noalloc(pos, vel, force, C.byref(consts), n, stream))
+
+
+NOALLOC_MAX_BODIES = 32768
 
 
 def move_collision(pos, vel, force, consts, n, stream=0):
