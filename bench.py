@@ -60,6 +60,10 @@ def args_parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ref-gpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--sweep-runs", type=int, default=64)
+    ap.add_argument("--sweep-steps", type=int, default=10)
+    ap.add_argument("--sweep-settle", type=int, default=100)
     return ap.parse_args()
 
 
@@ -211,6 +215,124 @@ def profile_traffic():
         return None
 
 
+SWEEP_STEPS_PER_IMPACT = 5000
+
+
+def sweep_section(gi, torch, wl, a):
+    """Batched sweep: 64 impacts (target N log-uniform in [4,096, 131,072],
+    impactor 0.1x, angle U[0,60], speed U[1,1.5] v_esc, spin U[0,0.8] of
+    breakup) stepped together -- one persistent force launch per step over
+    all runs (per-run offset tables), step loop captured in a CUDA graph,
+    decomposition autotuned per N bucket -- against the plain per-run path:
+    the same impacts one after another, unfused force pass + kick-drift per
+    step, no graph.  Timed over K steps, extrapolated to 5,000 steps per
+    impact."""
+    ctx = gi.Context(torch.cuda.current_device())
+    pos, vel, runs, specs = wl.sweep(gi, torch, nruns=a.sweep_runs, seed=4,
+                                     settle_steps=a.sweep_settle, ctx=ctx)
+    p = wl.params(gi)
+    K = max(2, a.sweep_steps)
+    inter = sum(r.n * (r.n - 1) for r in runs)
+    st = torch.cuda.Stream()
+    A = (torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda())
+    B = (torch.empty_like(A[0]), torch.empty_like(A[1]))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(st):
+        t_tune = time.perf_counter()
+        ctx.autotune(A[0].data_ptr(), A[1].data_ptr(), runs, p, st.cuda_stream)
+        t_tune = time.perf_counter() - t_tune
+        g = ctx.graph(A[0].data_ptr(), A[1].data_ptr(), B[0].data_ptr(), B[1].data_ptr(), runs,
+                      p, K, st.cuda_stream)
+        g.launch(st.cuda_stream)
+        e0.record(st)
+        g.launch(st.cuda_stream)
+        e1.record(st)
+        torch.cuda.synchronize()
+        t_batched = e0.elapsed_time(e1) / K
+        g.close()
+        # plain per-run path, one impact after another
+        t_plain = 0.0
+        for r in runs:
+            sl = slice(r.offset, r.offset + r.n)
+            P = A[0][sl].clone()
+            V = A[1][sl].clone()
+            F = torch.zeros_like(P)
+            one = gi.Run(0, r.n, r.nfe, 0, r.dt, r.dt_over_mass_fe, r.dt_over_mass_si, 0.0)
+            ctx.forces(P.data_ptr(), V.data_ptr(), F.data_ptr(), [one], p, st.cuda_stream)
+            ctx.move(P.data_ptr(), V.data_ptr(), F.data_ptr(), [one], st.cuda_stream)
+            torch.cuda.synchronize()
+            e0.record(st)
+            for _ in range(K):
+                ctx.forces(P.data_ptr(), V.data_ptr(), F.data_ptr(), [one], p, st.cuda_stream)
+                ctx.move(P.data_ptr(), V.data_ptr(), F.data_ptr(), [one], st.cuda_stream)
+            e1.record(st)
+            torch.cuda.synchronize()
+            t_plain += e0.elapsed_time(e1) / K
+        t_ref = ref_kernel_sweep_ms(gi, torch, A, runs, p, st)
+    ctx.close()
+    ns = sorted(r.n for r in runs)
+    per_hour = lambda ms: 3600.0 / (ms * 1e-3 * SWEEP_STEPS_PER_IMPACT) * len(runs)
+    ref = None
+    if t_ref is not None:
+        ref = {"ms_per_step": t_ref, "impacts_per_hour": per_hour(t_ref),
+               "batched_over_reference": t_ref / t_batched,
+               "what": "each impact alone through the reference's own kernels "
+                       "(getForcesCollisionSingleGPU + moveBodiesCollisionSingleGPU, sm_103a), "
+                       "N padded to a multiple of 256 with distant bodies, 2 steps timed"}
+    return {"runs": len(runs), "bodies": int(sum(ns)), "n_min": ns[0], "n_median": ns[len(ns) // 2],
+            "n_max": ns[-1], "interactions_per_step": inter, "steps_timed": K,
+            "steps_per_impact": SWEEP_STEPS_PER_IMPACT,
+            "batched_ms_per_step": t_batched, "plain_ms_per_step": t_plain,
+            "batched_interactions_per_s": inter / (t_batched * 1e-3),
+            "plain_interactions_per_s": inter / (t_plain * 1e-3),
+            "impacts_per_hour_batched": per_hour(t_batched),
+            "impacts_per_hour_plain": per_hour(t_plain),
+            "batched_over_plain": t_plain / t_batched, "autotune_s": round(t_tune, 2),
+            "reference_kernels": ref,
+            "settle_steps": a.sweep_settle,
+            "batched": "one persistent force launch per step over all runs, K-step CUDA graph",
+            "plain": "each impact alone: gi_forces + gi_move per step (unfused, no graph), sequential"}
+
+
+def ref_kernel_sweep_ms(gi, torch, A, runs, p, st, steps=2):
+    """Sum over runs of the reference kernels' per-step time (None if the
+    reference kernels are not built)."""
+    import ctypes as C
+    import oracle as orc
+    ref = orc.ref_lib()
+    if ref is None:
+        return None
+    mu = p.MassSi
+    rp = gi.params_from_material(1.0, 1.0, p.MassFe / mu, 1.0, 5.0 / mu**2, 1.5 / mu**2, 0.02,
+                                 0.01, 0.002, 0.001)
+    dt = 1e-3 * mu ** 0.5
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    total = 0.0
+    for r in runs:
+        nr = ((r.n + 255) // 256) * 256
+        P = torch.zeros((nr, 4), device="cuda")
+        V = torch.zeros((nr, 4), device="cuda")
+        P[:r.n] = A[0][r.offset:r.offset + r.n]
+        V[:r.n] = A[1][r.offset:r.offset + r.n]
+        if nr > r.n:
+            P[r.n:, 0] = 1e6 + 10.0 * torch.arange(nr - r.n, device="cuda", dtype=torch.float32)
+        F = torch.zeros_like(P)
+        fc = gi.collision_consts(rp, r.nfe)
+        mc = gi.MoveCollisionConsts(dt, dt / rp.MassFe, dt / rp.MassSi, r.nfe)
+        for k in range(steps + 1):
+            if k == 1:
+                e0.record(st)
+            assert ref.giref_forces_collision(P.data_ptr(), V.data_ptr(), F.data_ptr(), C.byref(fc),
+                                              nr, st.cuda_stream) == 0
+            assert ref.giref_move_collision(P.data_ptr(), V.data_ptr(), F.data_ptr(), C.byref(mc),
+                                            nr, st.cuda_stream) == 0
+        e1.record(st)
+        torch.cuda.synchronize()
+        total += e0.elapsed_time(e1) / steps
+    return total
+
+
 def run_ours(a):
     import numpy as np
     import torch
@@ -320,6 +442,7 @@ def run_ours(a):
         refgpu = None
         if not a.no_ref_gpu:
             refgpu = ref_gpu_baseline(gi, orc, torch, pos, vel, nfe, p)
+        sweep = None if a.no_sweep else sweep_section(gi, torch, wl, a)
         result = {
             "metric": "interactions/s", "value": value, "unit": "interactions/s", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -333,7 +456,7 @@ def run_ours(a):
                        "l2": "flushed between timed steps (256 MB write, outside the events)",
                        "parallelism": f"replicas x{world}"},
             "fp32_tflops": achieved, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "ref_gpu": refgpu, "clocks": clk, "gpu_launches": a.steps,
+            "ref_gpu": refgpu, "sweep": sweep, "clocks": clk, "gpu_launches": 7 * a.steps,
             "wall_s_timed_region": t_wall, "state_finite": state_ok,
             "step_ms_min_max": [min(step_ms), max(step_ms)],
         }

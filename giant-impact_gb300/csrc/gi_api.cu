@@ -1123,6 +1123,72 @@ extern "C" int gi_move_damped_separate(float *pos, float *vel, const float *forc
     return move_impl(pos, vel, force, r, 2, (cudaStream_t)stream);
 }
 
+// ---------------------------------------------------- graph-captured loops --
+
+struct gi_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int device = 0;
+};
+
+extern "C" int gi_graph_create(gi_ctx *c, float *pos_a, float *vel_a, float *pos_b, float *vel_b,
+                               const gi_run *runs, int nruns, const gi_pair_params *params,
+                               int nparams, int nsteps, void *stream, gi_graph **out)
+{
+    if (!c || !out) return fail(GI_ERR_INVALID_ARG, "NULL argument");
+    *out = nullptr;
+    if (nsteps < 1) return fail(GI_ERR_INVALID_ARG, "nsteps = %d", nsteps);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (s == nullptr)
+        return fail(GI_ERR_INVALID_ARG, "capture needs a non-default stream");
+    DeviceGuard g(c->device);
+    // One uncaptured step sizes every scratch buffer (capture cannot allocate);
+    // it steps a -> b, so the caller's state must be re-read from a: it is,
+    // because the captured loop reads a first and the step above never wrote a.
+    int st = gi_step_pingpong(c, pos_a, vel_a, pos_b, vel_b, runs, nruns, params, nparams, 1, stream);
+    if (st) return st;
+    GI_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    GI_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+    st = gi_step_pingpong(c, pos_a, vel_a, pos_b, vel_b, runs, nruns, params, nparams, nsteps, stream);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (st) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return cuda_fail(e, "cudaGraphInstantiate");
+    }
+    gi_graph *gr = new gi_graph();
+    gr->graph = graph;
+    gr->exec = exec;
+    gr->device = c->device;
+    *out = gr;
+    return GI_OK;
+}
+
+extern "C" int gi_graph_launch(gi_graph *gr, void *stream)
+{
+    if (!gr) return fail(GI_ERR_INVALID_ARG, "graph is NULL");
+    DeviceGuard g(gr->device);
+    GI_CUDA(cudaGraphLaunch(gr->exec, (cudaStream_t)stream), "cudaGraphLaunch");
+    return GI_OK;
+}
+
+extern "C" int gi_graph_destroy(gi_graph *gr)
+{
+    if (!gr) return GI_OK;
+    DeviceGuard g(gr->device);
+    cudaGraphExecDestroy(gr->exec);
+    cudaGraphDestroy(gr->graph);
+    delete gr;
+    return GI_OK;
+}
+
 // ------------------------------------------------------ internal helpers --
 
 int gi_internal_fail(int status, const char *msg) { return fail(status, "%s", msg); }

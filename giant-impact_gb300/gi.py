@@ -105,6 +105,10 @@ _SIGS = {
                  _P], C.c_int),
     "gi_step_pingpong": ([_P, _P, _P, _P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams),
                           C.c_int, C.c_int, _P], C.c_int),
+    "gi_graph_create": ([_P, _P, _P, _P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams),
+                         C.c_int, C.c_int, _P, C.POINTER(_P)], C.c_int),
+    "gi_graph_launch": ([_P, _P], C.c_int),
+    "gi_graph_destroy": ([_P], C.c_int),
     "gi_diag_fp64": ([_P, _P, _P, _P, C.c_int, C.POINTER(Run), C.POINTER(PairParams),
                       C.POINTER(C.c_double), _P], C.c_int),
     "gi_potential_fp64": ([_P, _P, C.POINTER(Run), C.c_int, C.POINTER(PairParams), C.c_int,
@@ -290,6 +294,15 @@ class Context:
         check(lib().gi_step_pingpong(self.h, pos_a, vel_a, pos_b, vel_b, ra, nr, pa, npar, nsteps,
                                      stream))
 
+    def graph(self, pos_a, vel_a, pos_b, vel_b, runs, params, nsteps, stream):
+        """Capture nsteps fused steps into a StepGraph (stream must not be 0)."""
+        ra, nr = _arr(runs, Run)
+        pa, npar = _arr(params, PairParams)
+        h = C.c_void_p()
+        check(lib().gi_graph_create(self.h, pos_a, vel_a, pos_b, vel_b, ra, nr, pa, npar, nsteps,
+                                    stream, C.byref(h)))
+        return StepGraph(h)
+
     def diag(self, pos, vel, run, params, label=None, scope=0, stream=0) -> list[float]:
         out = (C.c_double * 15)()
         check(lib().gi_diag_fp64(self.h, pos, vel, label, scope, C.byref(run), C.byref(params),
@@ -308,6 +321,27 @@ class Context:
         pa, npar = _arr(params, PairParams)
         check(lib().gi_run_host(self.h, pos_host, vel_host, ntotal, ra, nr, pa, npar, nsteps,
                                 stream))
+
+
+class StepGraph:
+    """A captured step loop (gi_graph); launch() advances every run."""
+
+    def __init__(self, h):
+        self.h = h
+
+    def launch(self, stream):
+        check(lib().gi_graph_launch(self.h, stream))
+
+    def close(self):
+        if self.h:
+            lib().gi_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def ic_uniform_ball(seed, n, radius=20.0, fe_fraction=0.3, mass_fe=1.0, mass_si=0.4,

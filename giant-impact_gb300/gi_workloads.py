@@ -3,6 +3,11 @@
   config1(...)   8,192 bodies uniform in a ball of radius 20 D, inner 30 % by
                  radius Fe; mFe = 1, mSi = 0.4, KFe = 5, KSi = 1.5,
                  KR 0.02 / 0.01, shell depth 0.002 / 0.001 D; v = 0; dt = 1e-3.
+  sweep(...)     a parameter sweep of many impacts packed into one array (one
+                 run per impact): target N log-uniform in [4,096, 131,072],
+                 impactor 0.1 x target, angle U[0, 60] deg, speed U[1.0, 1.5]
+                 x escape, spin U[0, 0.8] x breakup; bodies settled together
+                 in one batched damped step call.
   impact(...)    two-body impact: target (60,000) and impactor (6,000), each
                  built as a seeded ball and settled on the GPU with the damped
                  separate-body step (the reference's generate-target-impactor
@@ -130,3 +135,53 @@ def impact(gi, torch, n_t=60000, n_i=6000, seed=2, settle_steps=1500, spin_fract
            angle_deg=45.0, speed_factor=1.2, ctx=None):
     pos, vel, fet, fei = settle_pair(gi, torch, n_t, n_i, seed=seed, steps=settle_steps, ctx=ctx)
     return spin_and_place(pos, vel, n_t, n_i, fet, fei, spin_fraction, angle_deg, speed_factor)
+
+
+def sweep(gi, torch, nruns=64, seed=4, settle_steps=100, nmin=4096, nmax=131072, ctx=None,
+          spin_max=0.8, angle_max=60.0, speed_range=(1.0, 1.5)):
+    """Returns (pos, vel, runs, specs): all impacts packed back to back, one
+    gi.Run per impact (material order [Fe1, Fe2, Si1, Si2] inside each)."""
+    rng = np.random.default_rng(seed)
+    specs = []
+    for r in range(nruns):
+        nt = int(round(math.exp(rng.uniform(math.log(nmin), math.log(nmax)))))
+        ni = max(64, int(round(0.1 * nt)))
+        specs.append(dict(n_target=nt, n_impactor=ni, angle=float(rng.uniform(0.0, angle_max)),
+                          speed=float(rng.uniform(*speed_range)),
+                          spin=float(rng.uniform(0.0, spin_max))))
+    # raw bodies, all settled together: every body is its own run
+    bodies = []
+    for r, sp in enumerate(specs):
+        bodies.append(raw_body(gi, seed * 100003 + 2 * r, sp["n_target"], 0.0, 1.0))
+        bodies.append(raw_body(gi, seed * 100003 + 2 * r + 1, sp["n_impactor"], 2.0, 3.0))
+    pos = np.concatenate([b[0] for b in bodies])
+    vel = np.concatenate([b[1] for b in bodies])
+    offs = np.concatenate([[0], np.cumsum([len(b[0]) for b in bodies])[:-1]]).astype(int)
+    own = ctx is None
+    if own:
+        ctx = gi.Context(0)
+    p = params(gi)
+    if settle_steps > 0:
+        runs = [run_desc(gi, int(o), len(b[0]), b[2], 8.0) for o, b in zip(offs, bodies)]
+        dp = torch.from_numpy(pos).cuda()
+        dv = torch.from_numpy(vel).cuda()
+        ctx.step(dp.data_ptr(), dv.data_ptr(), runs, p, settle_steps)
+        torch.cuda.synchronize()
+        pos, vel = dp.cpu().numpy(), dv.cpu().numpy()
+    if own:
+        ctx.close()
+    out_p, out_v, out_runs = [], [], []
+    off = 0
+    for r, sp in enumerate(specs):
+        bt, bi = 2 * r, 2 * r + 1
+        nt, ni = sp["n_target"], sp["n_impactor"]
+        pp = np.concatenate([pos[offs[bt]:offs[bt] + nt], pos[offs[bi]:offs[bi] + ni]])
+        vv = np.concatenate([vel[offs[bt]:offs[bt] + nt], vel[offs[bi]:offs[bi] + ni]])
+        P, V, nfe = spin_and_place(pp, vv, nt, ni, bodies[bt][2], bodies[bi][2],
+                                   spin_fraction=sp["spin"], angle_deg=sp["angle"],
+                                   speed_factor=sp["speed"])
+        out_p.append(P)
+        out_v.append(V)
+        out_runs.append(run_desc(gi, off, nt + ni, nfe))
+        off += nt + ni
+    return np.concatenate(out_p), np.concatenate(out_v), out_runs, specs

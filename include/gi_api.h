@@ -280,6 +280,21 @@ int gi_step_pingpong(gi_ctx *ctx, float *pos_a, float *vel_a, float *pos_b,
                      const gi_pair_params *params, int nparams, int nsteps,
                      void *stream);
 
+/* Graph-captured step loop: captures nsteps fused steps of the given runs
+ * (gi_step_pingpong a -> b -> a ...) on `stream` (a non-default stream)
+ * into a CUDA graph; each gi_graph_launch then advances every run nsteps
+ * steps with one launch call.  Runs one uncaptured step first (a -> b) to
+ * size the scratch memory, which capture cannot allocate; the captured loop
+ * starts again from a.  The graph bakes in the buffers, runs and
+ * decomposition: rebuild it when they change.  After a launch the state is
+ * in b if nsteps is odd, in a if even. */
+typedef struct gi_graph gi_graph;
+int gi_graph_create(gi_ctx *ctx, float *pos_a, float *vel_a, float *pos_b, float *vel_b,
+                    const gi_run *runs, int nruns, const gi_pair_params *params, int nparams,
+                    int nsteps, void *stream, gi_graph **out);
+int gi_graph_launch(gi_graph *graph, void *stream);
+int gi_graph_destroy(gi_graph *graph);
+
 /* FP64 diagnostics of one run (synchronous: returns with out filled).
  * label (device, one byte per body of the whole array, may be NULL)
  * selects scope: 0 = all, 1 = label 1 or 2 (Earth + Moon), 2 = label 1

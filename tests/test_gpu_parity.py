@@ -261,6 +261,34 @@ def test_contacts_deterministic_and_bucket_independent(gi, torch_cuda):
     assert np.array_equal(f1[:, :3], f2[:, :3])
 
 
+def test_graph_step_loop_matches_pingpong(gi, torch_cuda):
+    """A captured graph of 4 fused steps over a small sweep gives exactly the
+    state of gi_step_pingpong, launch after launch."""
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    pos, vel, runs, _ = wl.sweep(gi, torch, nruns=5, seed=9, settle_steps=10, nmin=500, nmax=3000)
+    c = gi.Context(0)
+    s = torch.cuda.Stream()
+    a = (dev(torch, pos), dev(torch, vel))
+    b = (torch.empty_like(a[0]), torch.empty_like(a[1]))
+    with torch.cuda.stream(s):
+        g = c.graph(a[0].data_ptr(), a[1].data_ptr(), b[0].data_ptr(), b[1].data_ptr(), runs, p, 4,
+                    s.cuda_stream)
+        g.launch(s.cuda_stream)
+        g.launch(s.cuda_stream)
+    torch.cuda.synchronize()
+    x = (dev(torch, pos), dev(torch, vel))
+    y = (torch.empty_like(x[0]), torch.empty_like(x[1]))
+    c.step_pingpong(x[0].data_ptr(), x[1].data_ptr(), y[0].data_ptr(), y[1].data_ptr(), runs, p, 8)
+    torch.cuda.synchronize()
+    g.close()
+    c.close()
+    for r in runs:  # bodies outside runs are untouched either way
+        sl = slice(r.offset, r.offset + r.n)
+        assert torch.equal(a[0][sl], x[0][sl]) and torch.equal(a[1][sl], x[1][sl])
+
+
 def test_batch_invariance(gi, torch_cuda, ctx):
     """A run's forces are bit-identical alone and inside a batch."""
     torch = torch_cuda
