@@ -64,6 +64,11 @@ def args_parse():
     ap.add_argument("--sweep-runs", type=int, default=64)
     ap.add_argument("--sweep-steps", type=int, default=10)
     ap.add_argument("--sweep-settle", type=int, default=100)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=12)
+    ap.add_argument("--serve-steps", type=int, default=200)
+    ap.add_argument("--serve-round", type=int, default=50)
+    ap.add_argument("--serve-rate", type=float, default=2.0)
     return ap.parse_args()
 
 
@@ -333,6 +338,106 @@ def ref_kernel_sweep_ms(gi, torch, A, runs, p, st, steps=2):
     return total
 
 
+def _pct(xs, q):
+    import numpy as np
+    return float(np.percentile(np.asarray(xs, dtype=np.float64), q)) if xs else None
+
+
+def serve_section(gi, torch, wl, a):
+    """Serving loop: a seeded Poisson stream (rate a.serve_rate / s) of
+    impact runs, target N log-uniform in [8,192, 262,144] (impactor 0.1x,
+    angle / speed / spin drawn as in the sweep), each asking for
+    a.serve_steps steps.  Continuous batching: requests are submitted to
+    gi_server as they arrive (real time) and admitted by HBM budget (150 GB)
+    and slots (64); every round advances all live runs a.serve_round steps in
+    one force launch per step.  Plain per-run path: the same stream served
+    one run at a time (FIFO), unfused force + kick-drift per step; its
+    timeline uses each run's measured GPU service time.  Latency per 1,000
+    steps = (done - arrival) / (steps / 1000); service latency counts from
+    admission (batched) or start (plain)."""
+    import numpy as np
+    R = a.serve_requests
+    pos, vel, runs, specs = wl.sweep(gi, torch, nruns=R, seed=5, settle_steps=20, nmin=8192,
+                                     nmax=262144)
+    p = wl.params(gi)
+    rng = np.random.default_rng(5)
+    arrivals = np.cumsum(rng.exponential(1.0 / a.serve_rate, size=R))
+    arrivals -= arrivals[0]
+    per_k = a.serve_steps / 1000.0
+    # ---- continuous batching
+    srv = gi.Server(p, device=torch.cuda.current_device(), budget_bytes=150 << 30, max_live_runs=64,
+                    steps_per_round=a.serve_round)
+    ids, nxt = {}, 0
+    t0 = time.perf_counter()
+    done = {}
+    while len(done) < R:
+        now = time.perf_counter() - t0
+        while nxt < R and arrivals[nxt] <= now:
+            r = runs[nxt]
+            one = gi.Run(0, r.n, r.nfe, 0, r.dt, r.dt_over_mass_fe, r.dt_over_mass_si, 0.0)
+            ids[nxt] = srv.submit(pos[r.offset:r.offset + r.n], vel[r.offset:r.offset + r.n], one,
+                                  a.serve_steps)
+            nxt += 1
+        st = srv.stats()
+        if st.live == 0 and st.queued == 0:
+            if nxt < R:
+                time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
+            continue
+        srv.round()
+        for k, rid in ids.items():
+            if k not in done:
+                info = srv.query(rid)
+                if info.state == gi.REQ_DONE:
+                    done[k] = info
+    t_end = max(i.t_done for i in done.values())
+    t_origin = min(i.t_submit for i in done.values()) - arrivals[0]
+    inter = sum(r.n * (r.n - 1) for r in runs) * a.serve_steps
+    lat = [(done[k].t_done - (t_origin + arrivals[k])) / per_k for k in range(R)]
+    svc = [(done[k].t_done - done[k].t_admit) / per_k for k in range(R)]
+    batched = {"p50_s_per_1000_steps": _pct(lat, 50), "p99_s_per_1000_steps": _pct(lat, 99),
+               "service_p50_s_per_1000_steps": _pct(svc, 50),
+               "service_p99_s_per_1000_steps": _pct(svc, 99),
+               "interactions_per_s": inter / (t_end - t_origin), "makespan_s": t_end - t_origin,
+               "rounds": srv.stats().rounds}
+    srv.close()
+    # ---- plain per-run path, FIFO
+    ctx = gi.Context(torch.cuda.current_device())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clock, lat_p, svc_p, busy = 0.0, [], [], 0.0
+    for k, r in enumerate(runs):
+        P = torch.from_numpy(pos[r.offset:r.offset + r.n]).cuda()
+        V = torch.from_numpy(vel[r.offset:r.offset + r.n]).cuda()
+        F = torch.zeros_like(P)
+        one = gi.Run(0, r.n, r.nfe, 0, r.dt, r.dt_over_mass_fe, r.dt_over_mass_si, 0.0)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(a.serve_steps):
+            ctx.forces(P.data_ptr(), V.data_ptr(), F.data_ptr(), [one], p)
+            ctx.move(P.data_ptr(), V.data_ptr(), F.data_ptr(), [one])
+        e1.record()
+        torch.cuda.synchronize()
+        service = e0.elapsed_time(e1) * 1e-3
+        start = max(clock, arrivals[k])
+        clock = start + service
+        busy += service
+        lat_p.append((clock - arrivals[k]) / per_k)
+        svc_p.append(service / per_k)
+    ctx.close()
+    plain = {"p50_s_per_1000_steps": _pct(lat_p, 50), "p99_s_per_1000_steps": _pct(lat_p, 99),
+             "service_p50_s_per_1000_steps": _pct(svc_p, 50),
+             "service_p99_s_per_1000_steps": _pct(svc_p, 99),
+             "interactions_per_s": inter / clock, "makespan_s": clock}
+    ns = sorted(r.n for r in runs)
+    return {"requests": R, "steps_per_request": a.serve_steps, "arrival_rate_per_s": a.serve_rate,
+            "steps_per_round": a.serve_round, "n_min": ns[0], "n_median": ns[len(ns) // 2],
+            "n_max": ns[-1], "interactions": inter, "hbm_budget_gb": 150, "slots": 64,
+            "batched": batched, "plain": plain,
+            # interactions asked for per second of the arrival window, over what was served
+            "offered_over_served": (inter / max(arrivals[-1], 1e-9)) /
+                                   max(batched["interactions_per_s"], 1.0),
+            "plain_gpu_busy_s": busy}
+
+
 def run_ours(a):
     import numpy as np
     import torch
@@ -443,6 +548,7 @@ def run_ours(a):
         if not a.no_ref_gpu:
             refgpu = ref_gpu_baseline(gi, orc, torch, pos, vel, nfe, p)
         sweep = None if a.no_sweep else sweep_section(gi, torch, wl, a)
+        serve = None if a.no_serve else serve_section(gi, torch, wl, a)
         result = {
             "metric": "interactions/s", "value": value, "unit": "interactions/s", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -456,7 +562,7 @@ def run_ours(a):
                        "l2": "flushed between timed steps (256 MB write, outside the events)",
                        "parallelism": f"replicas x{world}"},
             "fp32_tflops": achieved, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "ref_gpu": refgpu, "sweep": sweep, "clocks": clk, "gpu_launches": 7 * a.steps,
+            "ref_gpu": refgpu, "sweep": sweep, "serve": serve, "clocks": clk, "gpu_launches": 7 * a.steps,
             "wall_s_timed_region": t_wall, "state_finite": state_ok,
             "step_ms_min_max": [min(step_ms), max(step_ms)],
         }

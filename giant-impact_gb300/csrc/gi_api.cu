@@ -1199,3 +1199,17 @@ int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d
     gi_params_from_collision_consts(c, &p);
     return to_device_params(p, *d);
 }
+
+// Device bytes of scratch one run of n bodies needs in this context (split-j
+// partials, contact corrections, grid): the serving loop's admission estimate.
+long long gi_internal_scratch_bytes(gi_ctx *c, int n)
+{
+    if (n <= 0) return 0;
+    int ipt = 1, jc = GI_NT, lg = 0, tiles = 0, nsplit = 1;
+    tuning_for(c, n, &ipt, &jc);
+    chunking(n, jc, &lg, &tiles, &nsplit);
+    const long long partials = nsplit > 1 ? (long long)nsplit * 3 * 8 * n : 0;
+    const long long contacts = 24LL * n + 8LL * n + 4LL * gi_grid_buckets(n) + 4LL * 8192;
+    const long long tickets = 4LL * ((n + GI_NT - 1) / GI_NT);
+    return partials + contacts + tickets;
+}

@@ -109,3 +109,5 @@ cudaError_t gi_launch_ffma_peak(float *sink, int blocks, int iters, cudaStream_t
 // reference collision struct.
 int gi_internal_fail(int status, const char *msg);
 int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d);
+// Device scratch bytes one run of n bodies needs in `ctx` (admission estimate).
+long long gi_internal_scratch_bytes(gi_ctx *ctx, int n);

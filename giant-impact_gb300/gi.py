@@ -77,6 +77,26 @@ class MoveSeparateConsts(C.Structure):
                 ("boarder1", C.c_int), ("boarder2", C.c_int), ("boarder3", C.c_int)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_longlong), ("max_live_runs", C.c_int),
+                ("steps_per_round", C.c_int)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int), ("n", C.c_int), ("steps_done", C.c_int), ("nsteps", C.c_int),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("bytes", C.c_longlong)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("live", C.c_int), ("queued", C.c_int), ("completed", C.c_longlong),
+                ("rounds", C.c_longlong), ("bytes_in_use", C.c_longlong),
+                ("pool_bodies", C.c_longlong), ("interactions", C.c_longlong)]
+
+
+SERVER_DRY_RUN = -1
+REQ_QUEUED, REQ_LIVE, REQ_DONE = 0, 1, 2
+
 _P = C.c_void_p
 _SIGS = {
     "gi_version": ([], C.c_int),
@@ -116,6 +136,14 @@ _SIGS = {
     "gi_run_host": ([_P, _P, _P, C.c_int, C.POINTER(Run), C.c_int, C.POINTER(PairParams),
                      C.c_int, C.c_int, _P], C.c_int),
     "gi_measure_ffma_peak": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
+    "gi_server_create": ([C.c_int, C.POINTER(ServerConfig), C.POINTER(PairParams), C.c_int,
+                          C.POINTER(_P)], C.c_int),
+    "gi_server_destroy": ([_P], C.c_int),
+    "gi_server_submit": ([_P, _P, _P, C.POINTER(Run), C.c_int, C.POINTER(C.c_longlong)], C.c_int),
+    "gi_server_round": ([_P, C.POINTER(C.c_int)], C.c_int),
+    "gi_server_query": ([_P, C.c_longlong, C.POINTER(RequestInfo)], C.c_int),
+    "gi_server_fetch": ([_P, C.c_longlong, _P, _P], C.c_int),
+    "gi_server_get_stats": ([_P, C.POINTER(ServerStats)], C.c_int),
     "gi_params_from_material": ([C.c_double] * 10 + [C.POINTER(PairParams)], C.c_int),
     "gi_params_from_collision_consts": ([C.POINTER(ForceCollisionConsts), C.POINTER(PairParams)],
                                         C.c_int),
@@ -342,6 +370,60 @@ class StepGraph:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """Continuous-batching serving loop (gi_server_*)."""
+
+    def __init__(self, params, device=0, budget_bytes=150 << 30, max_live_runs=64,
+                 steps_per_round=100):
+        pa, npar = _arr(params, PairParams)
+        cfg = ServerConfig(budget_bytes, max_live_runs, steps_per_round)
+        h = C.c_void_p()
+        check(lib().gi_server_create(device, C.byref(cfg), pa, npar, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().gi_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, pos, vel, run, nsteps) -> int:
+        import numpy as np
+        pos = np.ascontiguousarray(pos, np.float32)
+        vel = np.ascontiguousarray(vel, np.float32)
+        rid = C.c_longlong()
+        check(lib().gi_server_submit(self.h, pos.ctypes.data, vel.ctypes.data, C.byref(run), nsteps,
+                                     C.byref(rid)))
+        return rid.value
+
+    def round(self) -> int:
+        n = C.c_int()
+        check(lib().gi_server_round(self.h, C.byref(n)))
+        return n.value
+
+    def query(self, rid) -> RequestInfo:
+        info = RequestInfo()
+        check(lib().gi_server_query(self.h, rid, C.byref(info)))
+        return info
+
+    def fetch(self, rid, n):
+        import numpy as np
+        pos = np.zeros((n, 4), np.float32)
+        vel = np.zeros((n, 4), np.float32)
+        check(lib().gi_server_fetch(self.h, rid, pos.ctypes.data, vel.ctypes.data))
+        return pos, vel
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        check(lib().gi_server_get_stats(self.h, C.byref(st)))
+        return st
 
 
 def ic_uniform_ball(seed, n, radius=20.0, fe_fraction=0.3, mass_fe=1.0, mass_si=0.4,

@@ -326,6 +326,64 @@ int gi_run_host(gi_ctx *ctx, float *pos_host, float *vel_host, int ntotal,
 int gi_measure_ffma_peak(int device, double *tflops);
 
 /* ------------------------------------------------------------------------ */
+/* Serving loop (continuous batching of impact runs)                        */
+/* ------------------------------------------------------------------------ */
+
+/* Requests wait in a FIFO queue.  Each gi_server_round admits queued runs
+ * while a slot is free and their device memory (two state buffers plus the
+ * scratch estimate) fits in the HBM budget, advances every live run
+ * steps_per_round steps -- all live runs in one force launch per step --
+ * and retires finished runs to host memory.  A run's result is the same
+ * alone and in any mix (the force pass is batch-invariant).  The reference
+ * runs one impact per process; this has no counterpart there. */
+#define GI_SERVER_DRY_RUN (-1)   /* device value: schedule without a GPU */
+#define GI_REQ_QUEUED 0
+#define GI_REQ_LIVE 1
+#define GI_REQ_DONE 2
+
+typedef struct gi_server_config {
+    long long hbm_budget_bytes;  /* device memory the live runs may hold */
+    int max_live_runs;           /* slots */
+    int steps_per_round;         /* steps per round (latency granularity) */
+} gi_server_config;
+
+typedef struct gi_server_request_info {
+    int state;                   /* GI_REQ_* */
+    int n;
+    int steps_done;
+    int nsteps;
+    double t_submit, t_admit, t_done;  /* seconds, monotonic host clock */
+    long long bytes;             /* device bytes held while live */
+} gi_server_request_info;
+
+typedef struct gi_server_stats {
+    int live;
+    int queued;
+    long long completed;
+    long long rounds;
+    long long bytes_in_use;
+    long long pool_bodies;       /* capacity of the device state pool */
+    long long interactions;      /* pair interactions computed so far */
+} gi_server_stats;
+
+typedef struct gi_server gi_server;
+/* device = GI_SERVER_DRY_RUN runs the scheduling without a GPU (states are
+ * left unchanged, device memory is only accounted). */
+int gi_server_create(int device, const gi_server_config *cfg, const gi_pair_params *params,
+                     int nparams, gi_server **out);
+int gi_server_destroy(gi_server *srv);
+/* Copies the host bodies; run->offset is ignored, run->params indexes the
+ * server's pair table.  GI_ERR_CAPACITY if the run alone exceeds the budget. */
+int gi_server_submit(gi_server *srv, const float *pos_host, const float *vel_host,
+                     const gi_run *run, int nsteps, long long *id);
+/* One admit / step / retire round (synchronous). */
+int gi_server_round(gi_server *srv, int *nretired);
+int gi_server_query(gi_server *srv, long long id, gi_server_request_info *info);
+/* Copies a finished run's bodies out and forgets the request. */
+int gi_server_fetch(gi_server *srv, long long id, float *pos_host, float *vel_host);
+int gi_server_get_stats(gi_server *srv, gi_server_stats *out);
+
+/* ------------------------------------------------------------------------ */
 /* Parameter helpers (host only)                                            */
 /* ------------------------------------------------------------------------ */
 

@@ -1,0 +1,90 @@
+"""Scheduling logic of the serving loop, run without a GPU (dry-run server):
+admission by HBM budget and slots, FIFO order, exact step counts across
+rounds, pool reuse and accounting."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+
+def bodies(n, seed=0):
+    rng = np.random.default_rng(seed)
+    return rng.normal(size=(n, 4)).astype(np.float32), rng.normal(size=(n, 4)).astype(np.float32)
+
+
+def run(gi, n, nfe=None):
+    return gi.Run(0, n, n // 3 if nfe is None else nfe, 0, 1e-3, 1e-3, 2.5e-3, 0.0)
+
+
+@pytest.fixture
+def params(gi):
+    return gi.params_from_material()
+
+
+def test_budget_limits_live_runs_fifo(gi, params):
+    n = 1000
+    per_run = 2 * 2 * 16 * n  # two state buffers of pos + vel
+    srv = gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=2 * per_run, max_live_runs=8,
+                    steps_per_round=10)
+    ids = [srv.submit(*bodies(n, k), run(gi, n), 25) for k in range(3)]
+    assert srv.round() == 0
+    st = srv.stats()
+    assert (st.live, st.queued, st.bytes_in_use) == (2, 1, 2 * per_run)
+    assert [srv.query(i).state for i in ids] == [gi.REQ_LIVE, gi.REQ_LIVE, gi.REQ_QUEUED]
+    assert srv.round() == 0
+    assert srv.round() == 2          # 25 steps = 10 + 10 + 5
+    assert srv.query(ids[0]).steps_done == 25
+    assert srv.query(ids[2]).state == gi.REQ_QUEUED  # admitted at the next round
+    srv.round()
+    assert srv.query(ids[2]).state == gi.REQ_LIVE
+    for _ in range(3):
+        srv.round()
+    assert srv.query(ids[2]).state == gi.REQ_DONE
+    st = srv.stats()
+    assert st.completed == 3 and st.live == 0 and st.bytes_in_use == 0
+    assert st.interactions == 3 * 25 * n * (n - 1)
+    p, v = srv.fetch(ids[0], n)
+    assert np.array_equal(p, bodies(n, 0)[0])  # dry run leaves the state as it was
+    with pytest.raises(gi.GIError):
+        srv.query(ids[0])  # fetched requests are forgotten
+
+
+def test_slots_and_head_of_line(gi, params):
+    srv = gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=10**9, max_live_runs=2,
+                    steps_per_round=7)
+    ids = [srv.submit(*bodies(100 + k), run(gi, 100 + k), 7) for k in range(5)]
+    srv.round()
+    assert srv.stats().completed == 2 and srv.stats().queued == 3
+    big = gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=64 * 1000, max_live_runs=8,
+                    steps_per_round=5)
+    a = big.submit(*bodies(600), run(gi, 600), 10)   # 38,400 bytes
+    b = big.submit(*bodies(500), run(gi, 500), 10)   # 32,000: does not fit beside a
+    c = big.submit(*bodies(10), run(gi, 10), 10)     # would fit, but waits behind b (FIFO)
+    big.round()
+    assert [big.query(i).state for i in (a, b, c)] == [gi.REQ_LIVE, gi.REQ_QUEUED, gi.REQ_QUEUED]
+    with pytest.raises(gi.GIError) as e:
+        big.submit(*bodies(2000), run(gi, 2000), 1)  # more than the whole budget
+    assert e.value.status == 11
+
+
+def test_pool_reuse_and_zero_step_runs(gi, params):
+    srv = gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=10**10, max_live_runs=4,
+                    steps_per_round=3)
+    for wave in range(5):
+        ids = [srv.submit(*bodies(2000 + 37 * k), run(gi, 2000 + 37 * k), 3) for k in range(4)]
+        srv.round()
+        assert all(srv.query(i).state == gi.REQ_DONE for i in ids)
+    assert srv.stats().pool_bodies <= 65536  # ranges are reused, the pool does not creep
+    z = srv.submit(*bodies(5), run(gi, 5), 0)
+    srv.round()
+    assert srv.query(z).state == gi.REQ_DONE and srv.query(z).steps_done == 0
+
+
+def test_bad_requests(gi, params):
+    srv = gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=10**6)
+    with pytest.raises(gi.GIError):
+        srv.submit(*bodies(10), gi.Run(0, 10, 11, 0, 0, 0, 0, 0), 5)
+    with pytest.raises(gi.GIError):
+        srv.submit(*bodies(10), gi.Run(0, 10, 1, 3, 0, 0, 0, 0), 5)
+    with pytest.raises(gi.GIError):
+        srv.submit(*bodies(10), run(gi, 10), -1)
