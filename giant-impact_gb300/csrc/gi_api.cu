@@ -1088,6 +1088,14 @@ static int separate_runs(int b1, int b2, int b3, int n, gi_run r[2])
     return GI_OK;
 }
 
+extern "C" int gi_params_from_separate_consts(const gi_force_separate_consts *c,
+                                              gi_pair_params *out)
+{
+    if (!c || !out) return fail(GI_ERR_INVALID_ARG, "NULL argument");
+    separate_params(c, out);
+    return GI_OK;
+}
+
 extern "C" int gi_forces_separate(const float *pos, const float *vel, float *force,
                                   const gi_force_separate_consts *sc, int n, void *stream)
 {
@@ -1192,6 +1200,8 @@ extern "C" int gi_graph_destroy(gi_graph *gr)
 // ------------------------------------------------------ internal helpers --
 
 int gi_internal_fail(int status, const char *msg) { return fail(status, "%s", msg); }
+
+int gi_internal_ctx_device(gi_ctx *c) { return c ? c->device : -1; }
 
 int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d)
 {

@@ -253,6 +253,16 @@ size_t gi_grid_words(long long max_end, long long bodies)
     return 2 * (size_t)max_end + gi_grid_buckets(bodies) + 8192;
 }
 
+cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, cudaStream_t s)
+{
+    if (m == 0 || m > 1024u * 8192u) return cudaErrorInvalidValue;
+    const int sb = (int)((m + 1023) / 1024);
+    gi::scan_blocks<<<sb, 1024, 0, s>>>(a, (int)m, sums);
+    gi::scan_sums<<<1, 1024, 0, s>>>(sums, sb);
+    gi::scan_add<<<sb, 1024, 0, s>>>(a, (int)m, sums);
+    return cudaGetLastError();
+}
+
 cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const LaunchTable &tab,
                                long long bodies, int max_end, unsigned int *work,
                                long long *delta, int nsm, cudaStream_t s)

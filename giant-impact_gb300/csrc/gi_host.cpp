@@ -13,25 +13,9 @@
 
 namespace {
 
-// splitmix64 (Steele, Lea, Flood 2014; Vigna's public-domain constants):
-// a counter-based generator whose stream is fixed by the seed alone.
-struct Rng {
-    uint64_t s;
-    explicit Rng(uint64_t seed) : s(seed) {}
-    uint64_t next()
-    {
-        uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-        return z ^ (z >> 31);
-    }
-    // Uniform double in [0, 1) with 53 random bits.
-    double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
-};
-
 // Uniform point in the unit ball by rejection from the cube (no
 // transcendental functions, so bit-identical across hosts).
-void unit_ball(Rng &g, double &x, double &y, double &z)
+void unit_ball(gi_host::Rng &g, double &x, double &y, double &z)
 {
     for (;;) {
         x = 2.0 * g.uniform() - 1.0;
@@ -49,7 +33,7 @@ extern "C" int gi_ic_uniform_ball(unsigned long long seed, int n, double radius,
                                   int *nfe_out)
 {
     if (n < 0 || !(radius > 0.0) || !pos || !vel || !nfe_out) return GI_ERR_INVALID_ARG;
-    Rng g(seed);
+    gi_host::Rng g(seed);
     std::vector<float> fe, si;
     fe.reserve(3 * (size_t)n);
     si.reserve(3 * (size_t)n);
@@ -81,7 +65,7 @@ extern "C" int gi_ic_lattice(unsigned long long seed, int n, double spacing, dou
                              float *pos, float *vel)
 {
     if (n < 0 || nfe < 0 || nfe > n || !pos || !vel) return GI_ERR_INVALID_ARG;
-    Rng g(seed);
+    gi_host::Rng g(seed);
     int side = 1;
     while ((long long)side * side * side < n) ++side;
     for (int k = 0; k < n; ++k) {

@@ -111,3 +111,8 @@ int gi_internal_fail(int status, const char *msg);
 int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d);
 // Device scratch bytes one run of n bodies needs in `ctx` (admission estimate).
 long long gi_internal_scratch_bytes(gi_ctx *ctx, int n);
+// Device ordinal of a context (-1 for NULL).
+int gi_internal_ctx_device(gi_ctx *ctx);
+// gi_grid.cu: exclusive scan of m <= 1024 * 8192 counters in place; sums
+// holds 8192 words of scratch.
+cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, cudaStream_t s);

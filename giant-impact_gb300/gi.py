@@ -94,6 +94,60 @@ class ServerStats(C.Structure):
                 ("pool_bodies", C.c_longlong), ("interactions", C.c_longlong)]
 
 
+class SetupGenerating(C.Structure):
+    _fields_ = [("spin1", C.c_float * 4), ("spin2", C.c_float * 4),
+                ("frac_earth_mass1", C.c_double), ("frac_earth_mass2", C.c_double),
+                ("frac_fe1", C.c_double), ("frac_si1", C.c_double), ("frac_fe2", C.c_double),
+                ("frac_si2", C.c_double), ("damp1", C.c_float), ("damp2", C.c_float),
+                ("n", C.c_int), ("damp_time", C.c_double), ("damp_rest_time", C.c_double),
+                ("spin_rest_time", C.c_double), ("dt", C.c_double), ("density_fe", C.c_double),
+                ("density_si", C.c_double), ("k_fe", C.c_double), ("k_si", C.c_double),
+                ("kr_fe", C.c_double), ("kr_si", C.c_double), ("sd_fe", C.c_double),
+                ("sd_si", C.c_double), ("draw_rate", C.c_int)]
+
+
+class SetupImpactInit(C.Structure):
+    _fields_ = [("pos1", C.c_float * 3), ("pos2", C.c_float * 3), ("vel1", C.c_float * 3),
+                ("vel2", C.c_float * 3)]
+
+
+class SetupAddTime(C.Structure):
+    _fields_ = [("additional_time_days", C.c_double), ("dt", C.c_double),
+                ("draw_rate", C.c_int), ("record_rate", C.c_int), ("recenter_rate", C.c_int)]
+
+
+class BodyParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "unit_time", "unit_length", "unit_mass", "mass_fe", "mass_si", "diameter", "k_fe", "k_si",
+        "kr_fe", "kr_si", "sd_fe", "sd_si")] + [
+        (n, C.c_int) for n in ("n", "nfe1", "nsi1", "nfe2", "nsi2")]
+
+
+class GenerationPlan(C.Structure):
+    _fields_ = [("body", BodyParams), ("mass_body1", C.c_double), ("mass_body2", C.c_double),
+                ("damp_time", C.c_double), ("damp_rest_time", C.c_double),
+                ("spin_rest_time", C.c_double), ("spin1_w", C.c_float), ("spin2_w", C.c_float),
+                ("radius_of_earth", C.c_double)]
+
+
+class EarthMoon(C.Structure):
+    _fields_ = [("earth_label", C.c_int), ("moon_label", C.c_int), ("n_earth", C.c_int),
+                ("n_moon", C.c_int), ("n_groups", C.c_int), ("earth_counts", C.c_int * 4),
+                ("moon_counts", C.c_int * 4)]
+
+
+class GenerateReport(C.Structure):
+    _fields_ = [("steps", C.c_longlong), ("damped_steps", C.c_longlong),
+                ("rest_steps", C.c_longlong), ("spin_steps", C.c_longlong),
+                ("redraws", C.c_longlong), ("seconds", C.c_double)]
+
+
+class AddTimeReport(C.Structure):
+    _fields_ = [("steps", C.c_longlong), ("frames_written", C.c_longlong),
+                ("recenters", C.c_longlong), ("start_time", C.c_double),
+                ("end_time", C.c_double), ("seconds", C.c_double), ("earth_moon", EarthMoon)]
+
+
 SERVER_DRY_RUN = -1
 REQ_QUEUED, REQ_LIVE, REQ_DONE = 0, 1, 2
 
@@ -147,6 +201,50 @@ _SIGS = {
     "gi_params_from_material": ([C.c_double] * 10 + [C.POINTER(PairParams)], C.c_int),
     "gi_params_from_collision_consts": ([C.POINTER(ForceCollisionConsts), C.POINTER(PairParams)],
                                         C.c_int),
+    "gi_params_from_separate_consts": ([C.POINTER(ForceSeparateConsts), C.POINTER(PairParams)],
+                                       C.c_int),
+    "gi_read_setup_generating": ([C.c_char_p, C.POINTER(SetupGenerating)], C.c_int),
+    "gi_read_setup_impact_init": ([C.c_char_p, C.POINTER(SetupImpactInit)], C.c_int),
+    "gi_read_setup_add_time": ([C.c_char_p, C.POINTER(SetupAddTime)], C.c_int),
+    "gi_read_body_params": ([C.c_char_p, C.POINTER(BodyParams)], C.c_int),
+    "gi_write_body_params": ([C.c_char_p, C.POINTER(BodyParams)], C.c_int),
+    "gi_read_view_centering": ([C.c_char_p, C.POINTER(C.c_float)], C.c_int),
+    "gi_write_view_centering": ([C.c_char_p, C.POINTER(C.c_float)], C.c_int),
+    "gi_derive_units": ([C.POINTER(SetupGenerating), C.POINTER(GenerationPlan)], C.c_int),
+    "gi_collision_consts_from_body_params": ([C.POINTER(BodyParams), C.c_double,
+                                              C.POINTER(ForceCollisionConsts),
+                                              C.POINTER(MoveCollisionConsts)], C.c_int),
+    "gi_separate_consts_from_body_params": ([C.POINTER(BodyParams), C.c_double,
+                                             C.POINTER(ForceSeparateConsts),
+                                             C.POINTER(MoveSeparateConsts)], C.c_int),
+    "gi_write_body_file": ([C.c_char_p, _P, _P, C.c_int], C.c_int),
+    "gi_read_body_file": ([C.c_char_p, _P, _P, C.c_int, C.POINTER(C.c_int)], C.c_int),
+    "gi_frames_append": ([C.c_char_p, C.c_float, _P, _P, C.c_int], C.c_int),
+    "gi_frames_count": ([C.c_char_p, C.c_int, C.POINTER(C.c_longlong)], C.c_int),
+    "gi_frames_read": ([C.c_char_p, C.c_int, C.c_longlong, C.POINTER(C.c_float), _P, _P],
+                       C.c_int),
+    "gi_raw_bodies": ([C.c_ulonglong, C.POINTER(BodyParams), _P, _P, C.POINTER(C.c_longlong)],
+                      C.c_int),
+    "gi_spin_body": ([_P, _P, C.POINTER(GenerationPlan), C.c_int, C.POINTER(C.c_float),
+                      C.c_float], C.c_int),
+    "gi_zero_drift": ([_P, _P, C.POINTER(GenerationPlan)], C.c_int),
+    "gi_write_target_impactor_stats": ([C.c_char_p, C.POINTER(GenerationPlan),
+                                        C.POINTER(SetupGenerating), C.c_double, _P, _P], C.c_int),
+    "gi_impact_initial_conditions": ([C.POINTER(BodyParams), C.POINTER(SetupImpactInit), _P, _P,
+                                      _P, _P], C.c_int),
+    "gi_system_stats_host": ([_P, _P, C.c_int, C.c_int, C.c_double, C.c_double,
+                              C.POINTER(C.c_double)], C.c_int),
+    "gi_write_initial_stats": ([C.c_char_p, C.POINTER(BodyParams), C.POINTER(C.c_double)],
+                               C.c_int),
+    "gi_find_earth_moon": ([_P, _P, C.c_int, C.c_float, C.POINTER(C.c_int), _P, _P,
+                            C.POINTER(EarthMoon), _P], C.c_int),
+    "gi_write_run_stats": ([C.c_char_p, C.POINTER(BodyParams), C.c_double, C.POINTER(EarthMoon),
+                            C.POINTER(C.c_double)], C.c_int),
+    "gi_generate_target_impactor": ([C.c_int, C.c_char_p, C.c_char_p, C.c_ulonglong,
+                                     C.POINTER(GenerateReport)], C.c_int),
+    "gi_impact_initialize": ([C.c_char_p, C.c_char_p, C.c_char_p], C.c_int),
+    "gi_impact_add_time": ([C.c_int, C.c_char_p, C.c_char_p, C.c_char_p,
+                            C.POINTER(AddTimeReport)], C.c_int),
     "gi_ic_uniform_ball": ([C.c_ulonglong, C.c_int, C.c_double, C.c_double, C.c_float, C.c_float,
                             C.c_float, C.c_float, _P, _P, C.POINTER(C.c_int)], C.c_int),
     "gi_ic_lattice": ([C.c_ulonglong, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int,
@@ -448,3 +546,203 @@ def ic_lattice(seed, n, spacing=0.999, jitter=0.004, vel_sigma=1.0, nfe=None, ma
     check(lib().gi_ic_lattice(seed, n, spacing, jitter, vel_sigma, nfe, mass_fe, mass_si,
                               pos.ctypes.data, vel.ctypes.data))
     return pos, vel, nfe
+
+
+# ------------------------------------------------------------------ files --
+
+def _b(path) -> bytes:
+    return os.fsencode(path)
+
+
+def _f4(a, n=None):
+    """Contiguous float32 (n, 4) array and its address."""
+    import numpy as np
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if n is not None and a.shape != (n, 4):
+        raise ValueError(f"expected shape ({n}, 4), got {a.shape}")
+    return a, a.ctypes.data
+
+
+def read_setup_generating(path) -> SetupGenerating:
+    o = SetupGenerating()
+    check(lib().gi_read_setup_generating(_b(path), C.byref(o)))
+    return o
+
+
+def read_setup_impact_init(path) -> SetupImpactInit:
+    o = SetupImpactInit()
+    check(lib().gi_read_setup_impact_init(_b(path), C.byref(o)))
+    return o
+
+
+def read_setup_add_time(path) -> SetupAddTime:
+    o = SetupAddTime()
+    check(lib().gi_read_setup_add_time(_b(path), C.byref(o)))
+    return o
+
+
+def read_body_params(path) -> BodyParams:
+    o = BodyParams()
+    check(lib().gi_read_body_params(_b(path), C.byref(o)))
+    return o
+
+
+def write_body_params(path, b: BodyParams) -> None:
+    check(lib().gi_write_body_params(_b(path), C.byref(b)))
+
+
+def read_view_centering(path) -> list[float]:
+    v = (C.c_float * 6)()
+    check(lib().gi_read_view_centering(_b(path), v))
+    return list(v)
+
+
+def write_view_centering(path, v) -> None:
+    a = (C.c_float * 6)(*v)
+    check(lib().gi_write_view_centering(_b(path), a))
+
+
+def derive_units(setup: SetupGenerating) -> GenerationPlan:
+    o = GenerationPlan()
+    check(lib().gi_derive_units(C.byref(setup), C.byref(o)))
+    return o
+
+
+def collision_consts_from_body_params(b: BodyParams, dt: float):
+    fc, mc = ForceCollisionConsts(), MoveCollisionConsts()
+    check(lib().gi_collision_consts_from_body_params(C.byref(b), dt, C.byref(fc), C.byref(mc)))
+    return fc, mc
+
+
+def separate_consts_from_body_params(b: BodyParams, dt: float):
+    fc, mc = ForceSeparateConsts(), MoveSeparateConsts()
+    check(lib().gi_separate_consts_from_body_params(C.byref(b), dt, C.byref(fc), C.byref(mc)))
+    return fc, mc
+
+
+def params_from_separate_consts(c: ForceSeparateConsts) -> PairParams:
+    p = PairParams()
+    check(lib().gi_params_from_separate_consts(C.byref(c), C.byref(p)))
+    return p
+
+
+def write_body_file(path, pos, vel) -> None:
+    pa, pp = _f4(pos)
+    va, vp = _f4(vel, len(pa))
+    check(lib().gi_write_body_file(_b(path), pp, vp, len(pa)))
+
+
+def read_body_file(path):
+    import numpy as np
+    n = C.c_int()
+    check(lib().gi_read_body_file(_b(path), None, None, 0, C.byref(n)))
+    pos = np.zeros((n.value, 4), np.float32)
+    vel = np.zeros((n.value, 4), np.float32)
+    check(lib().gi_read_body_file(_b(path), pos.ctypes.data, vel.ctypes.data, n.value,
+                                  C.byref(n)))
+    return pos, vel
+
+
+def frames_append(path, time, pos, vel) -> None:
+    pa, pp = _f4(pos)
+    va, vp = _f4(vel, len(pa))
+    check(lib().gi_frames_append(_b(path), time, pp, vp, len(pa)))
+
+
+def frames_count(path, n) -> int:
+    k = C.c_longlong()
+    check(lib().gi_frames_count(_b(path), n, C.byref(k)))
+    return k.value
+
+
+def frames_read(path, n, frame=-1):
+    import numpy as np
+    t = C.c_float()
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    check(lib().gi_frames_read(_b(path), n, frame, C.byref(t), pos.ctypes.data, vel.ctypes.data))
+    return t.value, pos, vel
+
+
+def raw_bodies(seed, b: BodyParams):
+    """Returns (pos, vel, redraws) in the builder order [Fe1, Si1, Fe2, Si2]."""
+    import numpy as np
+    pos = np.zeros((b.n, 4), np.float32)
+    vel = np.zeros((b.n, 4), np.float32)
+    r = C.c_longlong()
+    check(lib().gi_raw_bodies(seed, C.byref(b), pos.ctypes.data, vel.ctypes.data, C.byref(r)))
+    return pos, vel, r.value
+
+
+def spin_body(pos, vel, plan: GenerationPlan, body, axis, w) -> None:
+    """In place on float32 (n, 4) numpy arrays."""
+    a = (C.c_float * 3)(*axis)
+    check(lib().gi_spin_body(pos.ctypes.data, vel.ctypes.data, C.byref(plan), body, a, w))
+
+
+def zero_drift(pos, vel, plan: GenerationPlan) -> None:
+    check(lib().gi_zero_drift(pos.ctypes.data, vel.ctypes.data, C.byref(plan)))
+
+
+def write_target_impactor_stats(path, plan, setup, dt, pos, vel) -> None:
+    pa, pp = _f4(pos)
+    va, vp = _f4(vel, len(pa))
+    check(lib().gi_write_target_impactor_stats(_b(path), C.byref(plan), C.byref(setup), dt, pp,
+                                               vp))
+
+
+def impact_initial_conditions(b: BodyParams, s: SetupImpactInit, pos, vel):
+    import numpy as np
+    pa, pp = _f4(pos, b.n)
+    va, vp = _f4(vel, b.n)
+    po = np.zeros((b.n, 4), np.float32)
+    vo = np.zeros((b.n, 4), np.float32)
+    check(lib().gi_impact_initial_conditions(C.byref(b), C.byref(s), pp, vp, po.ctypes.data,
+                                             vo.ctypes.data))
+    return po, vo
+
+
+def system_stats_host(pos, vel, nfe, mass_fe, mass_si) -> list[float]:
+    pa, pp = _f4(pos)
+    va, vp = _f4(vel, len(pa))
+    out = (C.c_double * 10)()
+    check(lib().gi_system_stats_host(pp, vp, len(pa), nfe, mass_fe, mass_si, out))
+    return list(out)
+
+
+def write_initial_stats(path, b: BodyParams, stats) -> None:
+    a = (C.c_double * 10)(*stats)
+    check(lib().gi_write_initial_stats(_b(path), C.byref(b), a))
+
+
+def find_earth_moon(ctx: "Context", pos, n, touch, bounds, group=None, scope=None,
+                    stream=0) -> EarthMoon:
+    """pos, group, scope: device pointers (group/scope may be None)."""
+    em = EarthMoon()
+    bd = (C.c_int * 3)(*bounds)
+    check(lib().gi_find_earth_moon(ctx.h, pos, n, touch, bd, group, scope, C.byref(em), stream))
+    return em
+
+
+def write_run_stats(path, b: BodyParams, time, em: EarthMoon, scope_stats) -> None:
+    flat = [float(x) for row in scope_stats for x in (list(row) + [0.0] * 15)[:15]]
+    a = (C.c_double * 60)(*flat)
+    check(lib().gi_write_run_stats(_b(path), C.byref(b), time, C.byref(em), a))
+
+
+def generate_target_impactor(setup_path, info_dir, seed=1, device=0) -> GenerateReport:
+    r = GenerateReport()
+    check(lib().gi_generate_target_impactor(device, _b(setup_path), _b(info_dir), seed,
+                                            C.byref(r)))
+    return r
+
+
+def impact_initialize(info_dir, setup_path, impact_info_dir) -> None:
+    check(lib().gi_impact_initialize(_b(info_dir), _b(setup_path), _b(impact_info_dir)))
+
+
+def impact_add_time(info_dir, setup_path, impact_dir, device=0) -> AddTimeReport:
+    r = AddTimeReport()
+    check(lib().gi_impact_add_time(device, _b(info_dir), _b(setup_path), _b(impact_dir),
+                                   C.byref(r)))
+    return r

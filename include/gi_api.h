@@ -421,6 +421,244 @@ int gi_ic_lattice(unsigned long long seed, int n, double spacing, double jitter,
                   double vel_sigma, int nfe, float mass_fe, float mass_si,
                   float *pos, float *vel);
 
+/* ------------------------------------------------------------------------ */
+/* Setup, parameter and body files (host only)                              */
+/*                                                                          */
+/* Text files are read the way the reference reads them: for each value in */
+/* a fixed order, skip past the next '=' and read one number; key names are */
+/* not checked.  Float fields are parsed as float, double fields as double. */
+/* Returns GI_ERR_IO when the file cannot be opened, GI_ERR_FORMAT when a   */
+/* value is missing or not a number.                                        */
+/* ------------------------------------------------------------------------ */
+
+/* setupGeneratingTargetImpactor
+ * (Code/GenerateTargetImpactorCode/generateTargetImpactor.cu:169-248). */
+typedef struct gi_setup_generating {
+    float spin1[4], spin2[4];          /* spin axis xyz, revolutions per hour */
+    double frac_earth_mass1, frac_earth_mass2;
+    double frac_fe1, frac_si1, frac_fe2, frac_si2;
+    float damp1, damp2;                /* damping rates of body 1 and 2      */
+    int n;                             /* TotalNumberOfElements              */
+    double damp_time, damp_rest_time, spin_rest_time;  /* hours             */
+    double dt;                         /* code time units                    */
+    double density_fe, density_si;     /* kg km^-3                           */
+    double k_fe, k_si;                 /* kg km^-1 s^-2                      */
+    double kr_fe, kr_si, sd_fe, sd_si;
+    int draw_rate;
+} gi_setup_generating;
+
+/* setupImpactInitialization (Code/ImpactCode/impactInitialization.cu:183-217):
+ * body offsets in km and velocities in km/s (float, as the reference). */
+typedef struct gi_setup_impact_init {
+    float pos1[3], pos2[3], vel1[3], vel2[3];
+} gi_setup_impact_init;
+
+/* setupImpactAddTime (Code/ImpactCode/impactAddTime.cu:40-75). */
+typedef struct gi_setup_add_time {
+    double additional_time_days;
+    double dt;
+    int draw_rate, record_rate, recenter_rate;
+} gi_setup_add_time;
+
+/* targetImpactorParameters, the file that carries the code units from the
+ * body builder to the impact drivers
+ * (generateTargetImpactorBasicFunctions.h:688-711 writes it,
+ * impactBasicFunctions.h:31-107 reads it). */
+typedef struct gi_body_params {
+    double unit_time, unit_length, unit_mass;  /* s, km, kg                   */
+    double mass_fe, mass_si, diameter;         /* code units                  */
+    double k_fe, k_si, kr_fe, kr_si, sd_fe, sd_si;
+    int n, nfe1, nsi1, nfe2, nsi2;
+} gi_body_params;
+
+/* What the body builder derives from its setup (setTargetImpactorParameters,
+ * generateTargetImpactor.cu:289-403). */
+typedef struct gi_generation_plan {
+    gi_body_params body;
+    double mass_body1, mass_body2;               /* code units (MassOfBody1/2) */
+    double damp_time, damp_rest_time, spin_rest_time;  /* code time units     */
+    float spin1_w, spin2_w;                      /* revolutions per time unit */
+    double radius_of_earth;                      /* code length units          */
+} gi_generation_plan;
+
+int gi_read_setup_generating(const char *path, gi_setup_generating *out);
+int gi_read_setup_impact_init(const char *path, gi_setup_impact_init *out);
+int gi_read_setup_add_time(const char *path, gi_setup_add_time *out);
+int gi_read_body_params(const char *path, gi_body_params *out);
+/* Same lines and "%f" / "%d" formats as the reference writer. */
+int gi_write_body_params(const char *path, const gi_body_params *p);
+/* viewCenteringInfo: initial centre of mass xyz, initial linear velocity xyz
+ * (impactInitialization.cu:515-532, impactBasicFunctions.h:1074-1086). */
+int gi_read_view_centering(const char *path, float out[6]);
+int gi_write_view_centering(const char *path, const float v[6]);
+
+/* Units, body counts and element masses from a setup (integer truncation of
+ * the counts as in the reference).  GI_ERR_PARAMS when a body's Fe and Si
+ * fractions do not add to 1 or there is no mass. */
+int gi_derive_units(const gi_setup_generating *setup, gi_generation_plan *out);
+
+/* The kernel constant structs the reference drivers load from the
+ * parameters: collision (impactAddTime.cu:106-166) and separate
+ * (generateTargetImpactor.cu:406-451), with the reference's float
+ * conversions.  dt in code time units. */
+int gi_collision_consts_from_body_params(const gi_body_params *b, double dt,
+                                         gi_force_collision_consts *fc,
+                                         gi_move_collision_consts *mc);
+int gi_separate_consts_from_body_params(const gi_body_params *b, double dt,
+                                        gi_force_separate_consts *fc,
+                                        gi_move_separate_consts *mc);
+/* Pair table of a reference separate struct (Si-Si gravity = 1). */
+int gi_params_from_separate_consts(const gi_force_separate_consts *c,
+                                   gi_pair_params *out);
+
+/* targetImpactorInitialPosVel: int n, n float4 positions, n float4
+ * velocities (generateTargetImpactorBasicFunctions.h:713-722).
+ * gi_read_body_file with pos or vel NULL only returns the count in *n. */
+int gi_write_body_file(const char *path, const float *pos, const float *vel, int n);
+int gi_read_body_file(const char *path, float *pos, float *vel, int capacity, int *n);
+
+/* impactPosVel: a sequence of frames, each float time, n float4 positions,
+ * n float4 velocities (impactInitialization.cu:373-378, impactAddTime.cu:424-428).
+ * gi_frames_read with frame = -1 reads the last frame, the point a resumed
+ * run starts from (impactAddTime.cu:207-241).  GI_ERR_FORMAT when the file
+ * size is not a whole number of frames. */
+int gi_frames_append(const char *path, float time, const float *pos, const float *vel, int n);
+int gi_frames_count(const char *path, int n, long long *nframes);
+int gi_frames_read(const char *path, int n, long long frame, float *time, float *pos,
+                   float *vel);
+
+/* ------------------------------------------------------------------------ */
+/* Body builder and impact set-up steps (host only)                         */
+/* ------------------------------------------------------------------------ */
+
+/* Raw target and impactor, order [Fe1, Si1, Fe2, Si2]
+ * (createRawTargetImpactor, generateTargetImpactorBasicFunctions.h:239-405):
+ * per body an Fe core of radius r1 and an Si shell from r1 + D to r2 + D,
+ * r1 / r2 the radii of 2x the volume of NFe / NFe + NSi spheres at 68 %
+ * packing; each element is a cube-normalised direction at a uniform radius,
+ * redrawn while it is closer than D to an earlier element of its own
+ * material group.  A seeded generator replaces the wall-clock-seeded rand().
+ * pos.w = 0, 1, 2, 3 (Fe1, Si1, Fe2, Si2); vel = 0, vel.w = element mass.
+ * *redraws (may be NULL) = the number of rejected draws. */
+int gi_raw_bodies(unsigned long long seed, const gi_body_params *b, float *pos, float *vel,
+                  long long *redraws);
+
+/* Adds the spin of one body about its centre of mass (spinBody,
+ * generateTargetImpactorBasicFunctions.h:407-470): body = 1 or 2, axis the
+ * spin axis (normalised here; GI_ERR_PARAMS if it is zero), w the rate in
+ * revolutions per code time unit. */
+int gi_spin_body(float *pos, float *vel, const gi_generation_plan *plan, int body,
+                 const float axis[3], float w);
+
+/* Moves each body's centre of mass to the origin and removes its mean
+ * velocity (zeroOutTargetImpactorDrift,
+ * generateTargetImpactorBasicFunctions.h:472-506).  Like the reference, the
+ * sums are divided by the body mass from the setup (MassOfBody1/2). */
+int gi_zero_drift(float *pos, float *vel, const gi_generation_plan *plan);
+
+/* targetImpactorStats (recordTargetImpactorStats,
+ * generateTargetImpactorBasicFunctions.h:590-686). */
+int gi_write_target_impactor_stats(const char *path, const gi_generation_plan *plan,
+                                   const gi_setup_generating *setup, double dt,
+                                   const float *pos, const float *vel);
+
+/* Impact initial conditions (setupInitialConditions,
+ * impactInitialization.cu:260-391): shift body 1 and body 2 by their setup
+ * offset and velocity (converted to code units in float as the reference
+ * does), then reorder [Fe1, Si1, Fe2, Si2] -> [Fe1, Fe2, Si1, Si2], so that
+ * index < NFe1 + NFe2 is Fe. */
+int gi_impact_initial_conditions(const gi_body_params *b, const gi_setup_impact_init *s,
+                                 const float *pos_in, const float *vel_in, float *pos_out,
+                                 float *vel_out);
+
+/* Whole-system mass, centre of mass, linear velocity and angular momentum in
+ * double, summed in index order as the reference's recordInitialImpactStat
+ * (impactInitialization.cu:393-474): out = [mass, com xyz, vel xyz, L xyz]. */
+int gi_system_stats_host(const float *pos, const float *vel, int n, int nfe, double mass_fe,
+                         double mass_si, double out[10]);
+
+/* initialStatsFile (impactInitialization.cu:476-513). stats as above. */
+int gi_write_initial_stats(const char *path, const gi_body_params *b, const double stats[10]);
+
+/* ------------------------------------------------------------------------ */
+/* Earth / Moon identification and the final statistics                    */
+/* ------------------------------------------------------------------------ */
+
+/* Result of gi_find_earth_moon.  Groups are the connected sets of bodies
+ * whose pairwise distance sqrtf(dx*dx + dy*dy + dz*dz) (FP32) is below
+ * touch; a group is named by its smallest body index, as the reference's
+ * group numbers are (findEarthAndMoon, impactBasicFunctions.h:109-217).
+ * The Earth is the largest group (the smallest name on a tie), the Moon the
+ * largest of the others (-1 / 0 when there is no other group).  Counts by
+ * origin are [Fe body 1, Fe body 2, Si body 1, Si body 2] of the
+ * [Fe1, Fe2, Si1, Si2] order (impactBasicFunctions.h:921-935). */
+typedef struct gi_earth_moon {
+    int earth_label, moon_label;
+    int n_earth, n_moon;
+    int n_groups;
+    int earth_counts[4];
+    int moon_counts[4];
+} gi_earth_moon;
+
+/* Groups on the GPU (hashed cell grid of cell size > touch, lock-free
+ * union-find); synchronous.  pos: device, n float4.  bounds = NFe1,
+ * NFe1 + NFe2, NFe1 + NFe2 + NSi1 for the origin counts.  group (device,
+ * n ints, may be NULL) receives each body's group name; scope (device, n
+ * bytes, may be NULL) receives 1 for Earth, 2 for Moon, 0 otherwise -- the
+ * label array gi_diag_fp64 takes.  touch is 1.5 D in the reference. */
+int gi_find_earth_moon(gi_ctx *ctx, const float *pos, int n, float touch, const int bounds[3],
+                       int *group, unsigned char *scope, gi_earth_moon *out, void *stream);
+
+/* runStatsFile (recordFinalImpactStat, impactBasicFunctions.h:883-1072):
+ * scope_stats[s] = gi_diag_fp64's out[0..9] for scope s = 0 (all),
+ * 1 (Earth + Moon), 2 (Earth), 3 (Moon); time in code units. */
+int gi_write_run_stats(const char *path, const gi_body_params *b, double time,
+                       const gi_earth_moon *em, const double scope_stats[4][15]);
+
+/* ------------------------------------------------------------------------ */
+/* Headless drivers (the reference programs without the viewer)            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct gi_generate_report {
+    long long steps;          /* steps taken: damped, damped rest, spin rest  */
+    long long damped_steps, rest_steps, spin_steps;
+    long long redraws;        /* rejected draws of the raw-body builder       */
+    double seconds;           /* wall time of the step loop                   */
+} gi_generate_report;
+
+/* generateTargetImpactor without the window (generateTargetImpactor.cu:666-775):
+ * reads setup_path, builds the raw bodies (seeded), runs the damped, damped
+ * rest and spin rest phases with the separate-body force (the two bodies do
+ * not feel each other), spinning both bodies when the spin rest starts,
+ * zeroes each body's drift and writes targetImpactorStats,
+ * targetImpactorParameters and targetImpactorInitialPosVel into info_dir. */
+int gi_generate_target_impactor(int device, const char *setup_path, const char *info_dir,
+                                unsigned long long seed, gi_generate_report *report);
+
+/* impactInitialization (impactInitialization.cu:535-542), host only: reads
+ * info_dir/targetImpactorParameters, info_dir/targetImpactorInitialPosVel and
+ * setup_path, and writes impactPosVel (frame 0), initialStatsFile and
+ * viewCenteringInfo into impact_info_dir. */
+int gi_impact_initialize(const char *info_dir, const char *setup_path,
+                         const char *impact_info_dir);
+
+typedef struct gi_add_time_report {
+    long long steps, frames_written, recenters;
+    double start_time, end_time;   /* code units                             */
+    double seconds;                /* wall time of the step loop             */
+    gi_earth_moon earth_moon;      /* groups of the final state              */
+} gi_add_time_report;
+
+/* impactAddTime without the window (impactAddTime.cu:396-579): resumes from
+ * the last frame of impact_dir/ImpactInformation/impactPosVel, steps with
+ * the collision force until AdditionalTime has passed, appends a frame
+ * every RecordRate steps, moves the system's centre of mass and velocity
+ * back to the viewCenteringInfo values every RecenterRate steps (sums in
+ * FP64 on the GPU), and at the end writes impact_dir/runStatsFile and
+ * rewrites viewCenteringInfo. */
+int gi_impact_add_time(int device, const char *info_dir, const char *setup_path,
+                       const char *impact_dir, gi_add_time_report *report);
+
 #ifdef __cplusplus
 }
 #endif

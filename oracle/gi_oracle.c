@@ -481,3 +481,139 @@ void gio_count_flips(const float *pos, const float *vel, const int *idx,
     out[0] = band_flips;
     out[1] = sep_flips;
 }
+
+/* ------------------------------------------------------------- groups -- */
+
+static inline int touching_ref(const f4 *P, int k, int j, float touch)
+{
+    /* host code of the reference: each product and sum rounded to float */
+    float dx = P[k].x - P[j].x;
+    float dy = P[k].y - P[j].y;
+    float dz = P[k].z - P[j].z;
+    float s = dx * dx;
+    s = s + dy * dy;
+    s = s + dz * dz;
+    return sqrtf(s) < touch;
+}
+
+void gio_groups_ref(const float *pos, int n, float touch, int *group_id)
+{
+    const f4 *P = (const f4 *)pos;
+    unsigned char *used = (unsigned char *)calloc((size_t)(n > 0 ? n : 1), 1);
+    for (int i = 0; i < n; ++i) group_id[i] = -1;
+    int group = 0;
+    for (int i = 0; i < n; ++i) {
+        if (group_id[i] == -1) {
+            group_id[i] = group;
+            int k = i;
+            while (k < n) {
+                if (group_id[k] == group && !used[k]) {
+                    for (int j = i; j < n; ++j)
+                        if (touching_ref(P, k, j, touch)) group_id[j] = group;
+                    used[k] = 1;
+                    k = i;
+                } else {
+                    ++k;
+                }
+            }
+        }
+        ++group; /* numbered by i even when i already had a group */
+    }
+    free(used);
+}
+
+static int uf_root(int *parent, int x)
+{
+    while (parent[x] != x) {
+        parent[x] = parent[parent[x]];
+        x = parent[x];
+    }
+    return x;
+}
+
+typedef struct { long long key; int idx; } cell_entry;
+
+static int cmp_cell(const void *a, const void *b)
+{
+    const cell_entry *x = (const cell_entry *)a, *y = (const cell_entry *)b;
+    if (x->key != y->key) return x->key < y->key ? -1 : 1;
+    return x->idx - y->idx;
+}
+
+static long long cell_key(long long cx, long long cy, long long cz)
+{
+    /* 21 bits per axis after an offset; cells are clamped, so far bodies share edge cells */
+    const long long off = 1 << 20;
+    cx = cx < -off ? -off : (cx >= off ? off - 1 : cx);
+    cy = cy < -off ? -off : (cy >= off ? off - 1 : cy);
+    cz = cz < -off ? -off : (cz >= off ? off - 1 : cz);
+    return ((cx + off) << 42) | ((cy + off) << 21) | (cz + off);
+}
+
+static long long cell_coord(float x, double inv)
+{
+    double f = floor((double)x * inv);
+    if (!(f >= -1e9)) f = -1e9;
+    if (f > 1e9) f = 1e9;
+    return (long long)f;
+}
+
+void gio_groups_uf(const float *pos, int n, float touch, int *group_id)
+{
+    const f4 *P = (const f4 *)pos;
+    if (n <= 0) return;
+    int *parent = (int *)malloc((size_t)n * sizeof(int));
+    cell_entry *cells = (cell_entry *)malloc((size_t)n * sizeof(cell_entry));
+    const double inv = 1.0 / (2.0 * (double)touch);
+    for (int i = 0; i < n; ++i) {
+        parent[i] = i;
+        cells[i].key = cell_key(cell_coord(P[i].x, inv), cell_coord(P[i].y, inv),
+                                cell_coord(P[i].z, inv));
+        cells[i].idx = i;
+    }
+    qsort(cells, (size_t)n, sizeof(cell_entry), cmp_cell);
+    for (int i = 0; i < n; ++i) {
+        const long long cx = cell_coord(P[i].x, inv), cy = cell_coord(P[i].y, inv),
+                        cz = cell_coord(P[i].z, inv);
+        for (int o = 0; o < 27; ++o) {
+            const long long key = cell_key(cx + o % 3 - 1, cy + (o / 3) % 3 - 1, cz + o / 9 - 1);
+            /* first entry with this key */
+            int lo = 0, hi = n;
+            while (lo < hi) {
+                int mid = (lo + hi) / 2;
+                if (cells[mid].key < key) lo = mid + 1; else hi = mid;
+            }
+            for (int s = lo; s < n && cells[s].key == key; ++s) {
+                const int j = cells[s].idx;
+                if (j <= i || !touching_ref(P, i, j, touch)) continue;
+                int a = uf_root(parent, i), b = uf_root(parent, j);
+                if (a == b) continue;
+                if (a < b) parent[b] = a; else parent[a] = b;
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i) group_id[i] = uf_root(parent, i);
+    free(parent);
+    free(cells);
+}
+
+void gio_earth_moon_ref(const int *group_id, int n, const int *bounds, int *out)
+{
+    int *size = (int *)calloc((size_t)(n > 0 ? n : 1), sizeof(int));
+    for (int j = 0; j < n; ++j) size[group_id[j]]++;
+    int earth = -1, n_earth = 0, moon = -1, n_moon = 0, groups = 0;
+    for (int g = 0; g < n; ++g) {
+        if (size[g] > 0) ++groups;
+        if (size[g] > n_earth) { n_earth = size[g]; earth = g; }
+    }
+    for (int g = 0; g < n; ++g)
+        if (size[g] > n_moon && g != earth) { n_moon = size[g]; moon = g; }
+    for (int k = 0; k < 13; ++k) out[k] = 0;
+    out[0] = earth; out[1] = moon; out[2] = n_earth; out[3] = n_moon; out[4] = groups;
+    for (int j = 0; j < n; ++j) {
+        int c = j < bounds[0] ? 0 : (j < bounds[1] ? 1 : (j < bounds[2] ? 2 : 3));
+        if (group_id[j] == earth) out[5 + c]++;
+        else if (group_id[j] == moon) out[9 + c]++;
+    }
+    free(size);
+}

@@ -107,6 +107,25 @@ void gio_count_flips(const float *pos, const float *vel, const int *idx,
                      int nidx, long long *out, const gio_run *runs, int nruns,
                      const gio_params *params, int sep_test, int nthreads);
 
+/* Groups of touching bodies, restated literally from findEarthAndMoon
+ * (Code/ImpactCode/impactBasicFunctions.h:109-155): group numbers are the
+ * index of the body that started each group, the FP32 distance is
+ * sqrtf((dx*dx + dy*dy) + dz*dz) < touch.  O(N^2); small N only.
+ * group_id[i] receives body i's group number. */
+void gio_groups_ref(const float *pos, int n, float touch, int *group_id);
+
+/* The same groups by an independent method (cell lists of size 2*touch and
+ * a sequential union-find that keeps the smallest index as the root). */
+void gio_groups_uf(const float *pos, int n, float touch, int *group_id);
+
+/* Earth / Moon choice and origin counts from group numbers
+ * (impactBasicFunctions.h:157-216, :921-935): Earth = first group number
+ * with the strictly largest size, Moon = first other with the strictly
+ * largest size.  bounds = NFe1, NFe1 + NFe2, NFe1 + NFe2 + NSi1.
+ * out[0..12] = earth, moon (-1 if none), n_earth, n_moon, number of
+ * non-empty groups, earth counts [Fe1, Fe2, Si1, Si2], moon counts. */
+void gio_earth_moon_ref(const int *group_id, int n, const int *bounds, int *out);
+
 /* Smallest float t with sqrtf(t) >= s (the r2 threshold equivalent to the
  * reference's  s <= sqrt(r2)  comparison). */
 float gio_r2_threshold(float s);

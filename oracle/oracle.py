@@ -57,6 +57,9 @@ def lib() -> C.CDLL:
         L.gio_diag_fp64.argtypes = [P, P, P, I, P, P, P]
         L.gio_count_flips.argtypes = [P, P, P, I, P, P, I, P, I, I]
         L.gio_r2_threshold.argtypes = [F]
+        L.gio_groups_ref.argtypes = [P, I, F, P]
+        L.gio_groups_uf.argtypes = [P, I, F, P]
+        L.gio_earth_moon_ref.argtypes = [P, I, P, P]
         L.gio_r2_threshold.restype = F
         _lib = L
     return _lib
@@ -208,3 +211,30 @@ def ref_lib():
         L.giref_struct_sizes.argtypes = [P]
         _ref = L
     return _ref
+
+
+def groups_ref(pos, touch=1.5):
+    """Group number of every body, the reference's literal O(N^2) loop."""
+    pos = _f32(pos)
+    out = np.zeros(len(pos), np.int32)
+    lib().gio_groups_ref(pos.ctypes.data, len(pos), touch, out.ctypes.data)
+    return out
+
+
+def groups_uf(pos, touch=1.5):
+    """Group numbers by cell lists + union-find (larger N)."""
+    pos = _f32(pos)
+    out = np.zeros(len(pos), np.int32)
+    lib().gio_groups_uf(pos.ctypes.data, len(pos), touch, out.ctypes.data)
+    return out
+
+
+def earth_moon_ref(group_id, bounds):
+    """dict(earth, moon, n_earth, n_moon, n_groups, earth_counts, moon_counts)."""
+    g = np.ascontiguousarray(group_id, dtype=np.int32)
+    b = np.ascontiguousarray(bounds, dtype=np.int32)
+    out = np.zeros(13, np.int32)
+    lib().gio_earth_moon_ref(g.ctypes.data, len(g), b.ctypes.data, out.ctypes.data)
+    return dict(earth=int(out[0]), moon=int(out[1]), n_earth=int(out[2]), n_moon=int(out[3]),
+                n_groups=int(out[4]), earth_counts=[int(x) for x in out[5:9]],
+                moon_counts=[int(x) for x in out[9:13]])
