@@ -69,6 +69,15 @@ def args_parse():
     ap.add_argument("--serve-steps", type=int, default=200)
     ap.add_argument("--serve-round", type=int, default=50)
     ap.add_argument("--serve-rate", type=float, default=2.0)
+    ap.add_argument("--advance", type=int, default=0,
+                    help="untimed steps before timing (times the impact's contact phase)")
+    ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--large-steps", type=int, default=4)
+    ap.add_argument("--study", choices=["drift", "precision"], default=None,
+                    help="run a study instead of the benchmark (prints one JSON line)")
+    ap.add_argument("--study-steps", type=int, default=None)
+    ap.add_argument("--study-every", type=int, default=100)
+    ap.add_argument("--subsample", type=int, default=65536)
     return ap.parse_args()
 
 
@@ -438,6 +447,259 @@ def serve_section(gi, torch, wl, a):
             "plain_gpu_busy_s": busy}
 
 
+def _pingpong(torch, pos, vel):
+    n = len(pos)
+    return [(torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda()),
+            (torch.empty((n, 4), dtype=torch.float32, device="cuda"),
+             torch.empty((n, 4), dtype=torch.float32, device="cuda"))]
+
+
+def large_n_section(gi, torch, wl, ctx, peak_sustained, a):
+    """One 1,153,434-body impact (1,048,576 + 104,858, the precision-study
+    state): the fused step autotuned for this N, per-step CUDA events, L2
+    flushed between steps."""
+    pos, vel, nfe = wl.precision_impact(gi, 3)
+    n = len(pos)
+    p = wl.params(gi)
+    run = wl.run_desc(gi, 0, n, nfe)
+    bufs = _pingpong(torch, pos, vel)
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    t0 = time.perf_counter()
+    ctx.autotune(bufs[0][0].data_ptr(), bufs[0][1].data_ptr(), [run], p, s)
+    tune_s = time.perf_counter() - t0
+
+    def one(k):
+        (pa, va), (pb, vb) = bufs[k % 2], bufs[(k + 1) % 2]
+        ctx.step_pingpong(pa.data_ptr(), va.data_ptr(), pb.data_ptr(), vb.data_ptr(), [run], p, 1,
+                          s)
+
+    for k in range(2):
+        one(k)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(a.large_steps)]
+    for k in range(a.large_steps):
+        flush.fill_(float(k))
+        evs[k][0].record(stream)
+        one(2 + k)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(e0.elapsed_time(e1) for e0, e1 in evs) / a.large_steps
+    inter = n * (n - 1)
+    ips = inter / (ms * 1e-3)
+    tflops = ips * FLOP_PER_INTERACTION / 1e12
+    ipt, jchunk = ctx.get_tuning(n)
+    return {"workload": "1,048,576-body target + 104,858-body impactor (config-1 density balls, "
+                        "spin 0.5, 45 deg, 1.2 v_esc), one fused step per launch",
+            "n_bodies": n, "steps": a.large_steps, "ms_per_step": ms, "value": ips,
+            "unit": "interactions/s", "fp32_tflops": tflops,
+            "frac_of_sustained_ffma": tflops / peak_sustained,
+            "tuning": {"i_per_thread": ipt, "jchunk": jchunk, "autotune_s": round(tune_s, 1)}}
+
+
+def _energy_l(ctx, dp, dv, run, params):
+    """FP64 total energy (KE + pair potential), total angular momentum,
+    momentum and angular momentum about the centre of mass of one run."""
+    import numpy as np
+    d = ctx.diag(dp.data_ptr(), dv.data_ptr(), run, params)
+    pe = ctx.potential(dp.data_ptr(), [run], params)[0]
+    M, c, u = d[0], np.array(d[1:4]), np.array(d[4:7])
+    L = np.array(d[7:10]) + M * np.cross(c, u)
+    return d[10] + pe, L, np.array(d[11:14]), np.array(d[7:10])
+
+
+def _drift(log):
+    import numpy as np
+    E0, L0 = log[0][1], np.array(log[0][2])
+    dE = [abs(e - E0) / abs(E0) for _, e, _ in log]
+    dL = [float(np.linalg.norm(np.array(l) - L0) / np.linalg.norm(L0)) for _, _, l in log]
+    return {"E0": E0, "L0": list(L0), "max_rel_dE": max(dE), "final_rel_dE": dE[-1],
+            "max_rel_dL": max(dL), "final_rel_dL": dL[-1],
+            "curve": [(log[i][0], dE[i], dL[i]) for i in range(len(log))
+                      if i % 10 == 0 or i == len(log) - 1]}
+
+
+def _pl(extra):
+    """Momentum drift (relative to sum m |v| at the start) and drift of the
+    angular momentum about the centre of mass."""
+    import numpy as np
+    P0, Lc0 = np.array(extra[0][1]), np.array(extra[0][2])
+    dP = [float(np.linalg.norm(np.array(P) - P0)) for _, P, _ in extra]
+    dLc = [float(np.linalg.norm(np.array(L) - Lc0) / np.linalg.norm(Lc0)) for _, _, L in extra]
+    return {"max_abs_dP": max(dP), "final_abs_dP": dP[-1], "max_rel_dLcom": max(dLc),
+            "final_rel_dLcom": dLc[-1]}
+
+
+def study_drift(a):
+    """Energy and angular-momentum drift of the 66,000-body impact: this
+    library's fused step and the reference's own kernels from the same
+    settled state, FP64 diagnostics every `every` steps."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    gi = _load("gi", os.path.join(PKG, "gi.py"))
+    wl = _load("gi_workloads", os.path.join(PKG, "gi_workloads.py"))
+    import oracle as orc
+    steps = a.study_steps or 20000
+    every = a.study_every
+    ctx = gi.Context(0)
+    pos, vel, nfe = make_workload(gi, torch, wl, 2, a.settle_steps)
+    n = len(pos)
+    p = wl.params(gi)
+    run = wl.run_desc(gi, 0, n, nfe)
+    out = {"study": "drift", "workload": "plain two-body impact, 66,000 bodies, dt 1e-3",
+           "steps": steps, "every": every}
+    # this library: fused step, config units
+    dp, dv = torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda()
+    log, ms, extra = [], 0.0, []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for k in range(0, steps + 1, every):
+        if k:
+            e0.record()
+            ctx.step(dp.data_ptr(), dv.data_ptr(), [run], p, every)
+            e1.record()
+            torch.cuda.synchronize()
+            ms += e0.elapsed_time(e1)
+        E, L, P, Lc = _energy_l(ctx, dp, dv, run, p)
+        log.append((k, E, list(L)))
+        extra.append((k, list(P), list(Lc)))
+    out["ours"] = dict(_drift(log), ms_per_step=ms / steps, **_pl(extra))
+    # the reference's kernels: reference units (m_Si = 1), N padded to 256
+    ref = orc.ref_lib()
+    if ref is None:
+        out["reference"] = {"unavailable": "reference kernels not built"}
+    else:
+        mu = p.MassSi
+        rp = gi.params_from_material(1.0, 1.0, p.MassFe / mu, 1.0, 5.0 / mu**2, 1.5 / mu**2, 0.02,
+                                     0.01, 0.002, 0.001)
+        nr = ((n + 255) // 256) * 256
+        pp = np.zeros((nr, 4), np.float32)
+        vv = np.zeros((nr, 4), np.float32)
+        pp[:n], vv[:n] = pos, vel / np.float32([mu ** 0.5, mu ** 0.5, mu ** 0.5, 1.0])
+        pp[n:, :3] = 1e6 + np.arange(nr - n)[:, None] * 10.0
+        vv[n:, 3] = 1.0
+        fc = gi.collision_consts(rp, nfe)
+        dt = 1e-3 * mu ** 0.5
+        mc = gi.MoveCollisionConsts(dt, dt / rp.MassFe, dt / rp.MassSi, nfe)
+        rrun = wl.run_desc(gi, 0, n, nfe)
+        dp, dv = torch.from_numpy(pp).cuda(), torch.from_numpy(vv).cuda()
+        df = torch.zeros_like(dp)
+        s = torch.cuda.current_stream().cuda_stream
+        log, ms, extra = [], 0.0, []
+        for k in range(0, steps + 1, every):
+            if k:
+                e0.record()
+                for _ in range(every):
+                    assert ref.giref_forces_collision(dp.data_ptr(), dv.data_ptr(), df.data_ptr(),
+                                                      C.byref(fc), nr, s) == 0
+                    assert ref.giref_move_collision(dp.data_ptr(), dv.data_ptr(), df.data_ptr(),
+                                                    C.byref(mc), nr, s) == 0
+                e1.record()
+                torch.cuda.synchronize()
+                ms += e0.elapsed_time(e1)
+            E, L, P, Lc = _energy_l(ctx, dp, dv, rrun, rp)
+            log.append((k, E, list(L)))
+            extra.append((k, list(P), list(Lc)))
+        out["reference"] = dict(_drift(log), ms_per_step=ms / steps, **_pl(extra),
+                                what="getForcesCollisionSingleGPU + moveBodiesCollisionSingleGPU "
+                                     "from the reference sources, sm_103a, reference units, "
+                                     f"N padded to {nr} with distant bodies")
+    ctx.close()
+    print(json.dumps(out))
+    return out
+
+
+def study_precision(a):
+    """Large-N precision: force error of the three accumulation modes (and of
+    the reference's kernel) against the FP64 oracle on a seeded i-subsample
+    of the 1,153,434-body impact, then energy / angular-momentum drift of
+    each mode over `steps` fused steps."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    gi = _load("gi", os.path.join(PKG, "gi.py"))
+    wl = _load("gi_workloads", os.path.join(PKG, "gi_workloads.py"))
+    import oracle as orc
+    steps = a.study_steps or 100
+    pos, vel, nfe = wl.precision_impact(gi, 3)
+    n = len(pos)
+    p = wl.params(gi)
+    run = wl.run_desc(gi, 0, n, nfe)
+    idx = np.sort(np.random.default_rng(3).choice(n, min(a.subsample, n), replace=False)).astype(
+        np.int32)
+    t0 = time.perf_counter()
+    f64, _ = orc.forces_fp64(pos, vel, [(0, n, nfe, 0, 0, 0, 0, 0)], p, idx=idx)
+    t_oracle = time.perf_counter() - t0
+    scale = np.sqrt((f64 ** 2).sum(1))
+    out = {"study": "precision", "n_bodies": n, "subsample": len(idx), "steps": steps,
+           "oracle": {"what": "FP64 pair law (oracle/gi_oracle.c), OpenMP",
+                      "threads": orc.max_threads(), "seconds": round(t_oracle, 1)}}
+
+    def errors(f):
+        d = f[idx, :3].astype(np.float64) - f64
+        rel = np.sqrt((d ** 2).sum(1)) / np.maximum(scale, 1e-300)
+        return {"rel_l2": float(np.sqrt((d ** 2).sum() / (f64 ** 2).sum())),
+                "median_rel": float(np.median(rel)), "p99_rel": float(np.quantile(rel, 0.99)),
+                "max_rel": float(rel.max())}
+
+    modes = [("fp32", gi.GI_ACCUM_FP32), ("kahan", gi.GI_ACCUM_KAHAN), ("fp64", gi.GI_ACCUM_FP64)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, mode in modes:
+        ctx = gi.Context(0, accum=mode)
+        dp, dv = torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda()
+        df = torch.zeros_like(dp)
+        ctx.forces(dp.data_ptr(), dv.data_ptr(), df.data_ptr(), [run], p)  # warm-up
+        e0.record()
+        ctx.forces(dp.data_ptr(), dv.data_ptr(), df.data_ptr(), [run], p)
+        e1.record()
+        torch.cuda.synchronize()
+        res = errors(df.cpu().numpy())
+        res["force_ms"] = e0.elapsed_time(e1)
+        log = []
+        E, L, _, _ = _energy_l(ctx, dp, dv, run, p)
+        log.append((0, E, list(L)))
+        e0.record()
+        ctx.step(dp.data_ptr(), dv.data_ptr(), [run], p, steps)
+        e1.record()
+        torch.cuda.synchronize()
+        res["step_ms"] = e0.elapsed_time(e1) / steps
+        E, L, _, _ = _energy_l(ctx, dp, dv, run, p)
+        log.append((steps, E, list(L)))
+        dr = _drift(log)
+        res.update({k: dr[k] for k in ("E0", "final_rel_dE", "final_rel_dL")})
+        out[name] = res
+        ctx.close()
+    ref = orc.ref_lib()
+    if ref is not None:
+        mu = p.MassSi
+        rp = gi.params_from_material(1.0, 1.0, p.MassFe / mu, 1.0, 5.0 / mu**2, 1.5 / mu**2, 0.02,
+                                     0.01, 0.002, 0.001)
+        nr = ((n + 255) // 256) * 256
+        pp = np.zeros((nr, 4), np.float32)
+        vv = np.zeros((nr, 4), np.float32)
+        pp[:n], vv[:n] = pos, vel / np.float32([mu ** 0.5, mu ** 0.5, mu ** 0.5, 1.0])
+        pp[n:, :3] = 1e7 + np.arange(nr - n)[:, None] * 10.0
+        vv[n:, 3] = 1.0
+        fc = gi.collision_consts(rp, nfe)
+        dp, dv = torch.from_numpy(pp).cuda(), torch.from_numpy(vv).cuda()
+        df = torch.zeros_like(dp)
+        s = torch.cuda.current_stream().cuda_stream
+        e0.record()
+        assert ref.giref_forces_collision(dp.data_ptr(), dv.data_ptr(), df.data_ptr(), C.byref(fc),
+                                          nr, s) == 0
+        e1.record()
+        torch.cuda.synchronize()
+        f = df.cpu().numpy()[:n] * np.float32(mu ** 2)  # back to config units (F' = F / mu^2)
+        res = errors(f)
+        res["force_ms"] = e0.elapsed_time(e1)
+        res["what"] = f"reference getForcesCollisionSingleGPU, N padded to {nr}"
+        out["reference_kernel"] = res
+    print(json.dumps(out))
+    return out
+
+
 def run_ours(a):
     import numpy as np
     import torch
@@ -467,6 +729,9 @@ def run_ours(a):
         (pa, va), (pb, vb) = bufs[k % 2], bufs[(k + 1) % 2]
         ctx.step_pingpong(pa.data_ptr(), va.data_ptr(), pb.data_ptr(), vb.data_ptr(), [run], p, 1, s)
 
+    if a.advance > 0:  # evolve into the collision (untimed)
+        ctx.step(bufs[0][0].data_ptr(), bufs[0][1].data_ptr(), [run], p, a.advance, s)
+        torch.cuda.synchronize()
     # autotune the decomposition for this N on these bodies (setup, untimed)
     t_tune = time.perf_counter()
     ctx.autotune(bufs[0][0].data_ptr(), bufs[0][1].data_ptr(), [run], p, s)
@@ -547,6 +812,7 @@ def run_ours(a):
         refgpu = None
         if not a.no_ref_gpu:
             refgpu = ref_gpu_baseline(gi, orc, torch, pos, vel, nfe, p)
+        large = None if a.no_large else large_n_section(gi, torch, wl, ctx, peak_sustained, a)
         sweep = None if a.no_sweep else sweep_section(gi, torch, wl, a)
         serve = None if a.no_serve else serve_section(gi, torch, wl, a)
         result = {
@@ -557,12 +823,13 @@ def run_ours(a):
             "config": {"workload": "plain two-body impact: 60,000-body target + 6,000-body impactor, "
                                    "30% Fe, spin 0.5 breakup, 45 deg, 1.2 v_esc, dt 1e-3",
                        "n_bodies": n, "interactions_per_step": inter,
+                       "advance_steps": a.advance,
                        "accumulation": "kahan (FP32 tiles of 128, compensated across tiles)",
                        "tuning": {"i_per_thread": ipt, "jchunk": jchunk, "autotune_s": round(t_tune, 2)},
                        "l2": "flushed between timed steps (256 MB write, outside the events)",
                        "parallelism": f"replicas x{world}"},
             "fp32_tflops": achieved, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "ref_gpu": refgpu, "sweep": sweep, "serve": serve, "clocks": clk, "gpu_launches": 7 * a.steps,
+            "ref_gpu": refgpu, "large_n": large, "sweep": sweep, "serve": serve, "clocks": clk, "gpu_launches": 7 * a.steps,
             "wall_s_timed_region": t_wall, "state_finite": state_ok,
             "step_ms_min_max": [min(step_ms), max(step_ms)],
         }
@@ -639,7 +906,11 @@ def run_reference(a):
 
 if __name__ == "__main__":
     args = args_parse()
-    if args.impl == "reference":
+    if args.study == "drift":
+        study_drift(args)
+    elif args.study == "precision":
+        study_precision(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

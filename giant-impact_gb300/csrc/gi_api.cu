@@ -910,7 +910,7 @@ extern "C" int gi_diag_fp64(gi_ctx *c, const float *pos, const float *vel,
                             const gi_pair_params *params, double *out, void *stream)
 {
     if (!c || !run || !params || !out) return fail(GI_ERR_INVALID_ARG, "NULL argument");
-    if (scope < 0 || scope > 3) return fail(GI_ERR_INVALID_ARG, "scope %d", scope);
+    if (scope < 0 || scope > 4) return fail(GI_ERR_INVALID_ARG, "scope %d", scope);
     gi_run q = *run;
     q.params = 0;
     int st = check_runs(&q, 1, 1);

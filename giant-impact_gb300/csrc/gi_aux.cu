@@ -40,7 +40,8 @@ __device__ __forceinline__ bool in_scope(const unsigned char *label, int i, int 
     const unsigned char l = label[i];
     if (scope == 1) return l == 1 || l == 2;
     if (scope == 2) return l == 1;
-    return l == 2;
+    if (scope == 3) return l == 2;
+    return l == 3;
 }
 
 template <int NV>

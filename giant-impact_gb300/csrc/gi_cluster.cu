@@ -310,3 +310,123 @@ extern "C" int gi_find_earth_moon(gi_ctx *ctx, const float *pos, int n, float to
     }
     return GI_OK;
 }
+
+// ------------------------------------------------------------------ disk --
+
+namespace gi {
+
+// Largest distance of an Earth element (scope 1) from the Earth's centre of
+// mass, as the bits of a non-negative double (ordered like the value).
+__global__ void __launch_bounds__(256)
+earth_radius_kernel(const float4 *__restrict__ pos, const unsigned char *__restrict__ scope, int off,
+                    int n, double cx, double cy, double cz, unsigned long long *__restrict__ rmax)
+{
+    double m = 0.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = off + k;
+        if (scope[i] != 1) continue;
+        const float4 p = pos[i];
+        const double dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+        m = fmax(m, sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.0) atomicMax(rmax, (unsigned long long)__double_as_longlong(m));
+}
+
+// counts: [disk, bound inside, unbound]
+__global__ void __launch_bounds__(256)
+disk_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+            unsigned char *__restrict__ scope, int off, int n, double cx, double cy, double cz,
+            double ux, double uy, double uz, double gm, const unsigned long long *__restrict__ rmax,
+            int *__restrict__ counts)
+{
+    __shared__ int sc[3];
+    if (threadIdx.x < 3) sc[threadIdx.x] = 0;
+    __syncthreads();
+    const double R = __longlong_as_double((long long)*rmax) + 0.5;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const int i = off + k;
+        const unsigned char s = scope[i];
+        if (s == 1 || s == 2) continue;
+        const float4 p = pos[i], u = vel[i];
+        const double rx = p.x - cx, ry = p.y - cy, rz = p.z - cz;
+        const double vx = u.x - ux, vy = u.y - uy, vz = u.z - uz;
+        const double r = sqrt(rx * rx + ry * ry + rz * rz);
+        const double eps = 0.5 * (vx * vx + vy * vy + vz * vz) - gm / r;
+        const double hx = ry * vz - rz * vy, hy = rz * vx - rx * vz, hz = rx * vy - ry * vx;
+        const double req = (hx * hx + hy * hy + hz * hz) / gm;
+        int c;
+        if (eps < 0.0) c = req > R ? 0 : 1;
+        else c = 2;
+        scope[i] = c == 0 ? 3 : 0;
+        atomicAdd(&sc[c], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < 3 && sc[threadIdx.x]) atomicAdd(&counts[threadIdx.x], sc[threadIdx.x]);
+}
+
+}  // namespace gi
+
+extern "C" int gi_find_disk(gi_ctx *ctx, const float *pos, const float *vel, const gi_run *run,
+                            const gi_pair_params *params, unsigned char *scope, gi_disk_info *out,
+                            void *stream)
+{
+    if (!ctx || !pos || !vel || !run || !params || !scope || !out)
+        return gi_internal_fail(GI_ERR_INVALID_ARG, "gi_find_disk: NULL argument");
+    if (run->n < 0 || run->offset < 0)
+        return gi_internal_fail(GI_ERR_BAD_SIZE, "gi_find_disk: bad run");
+    if (!(params->MassSi > 0.0f) || !(params->GMassSiSi > 0.0f))
+        return gi_internal_fail(GI_ERR_PARAMS, "gi_find_disk: masses and gravity must be positive");
+    std::memset(out, 0, sizeof *out);
+    double earth[15];
+    if (int st = gi_diag_fp64(ctx, pos, vel, scope, 2, run, params, earth, stream)) return st;
+    out->earth_mass = earth[0];
+    if (run->n == 0 || !(earth[0] > 0.0)) return GI_OK;  // no Earth: nothing is bound to it
+    const double G = (double)params->GMassSiSi / ((double)params->MassSi * params->MassSi);
+    const int dev = gi_internal_ctx_device(ctx);
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+    struct Restore {
+        int prev, dev;
+        ~Restore()
+        {
+            if (prev != dev && prev >= 0) cudaSetDevice(prev);
+        }
+    } restore{prev, dev};
+    cudaStream_t s = (cudaStream_t)stream;
+    struct Res {
+        unsigned long long rmax;
+        int counts[3];
+        int pad;
+    };
+    Res *res = nullptr;
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&res), sizeof(Res), s);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMallocAsync");
+    Res host{};
+    const int blocks = std::min((run->n + 255) / 256, 4096);
+    const float4 *P = reinterpret_cast<const float4 *>(pos);
+    do {
+        if ((e = cudaMemsetAsync(res, 0, sizeof(Res), s)) != cudaSuccess) break;
+        gi::earth_radius_kernel<<<blocks, 256, 0, s>>>(P, scope, run->offset, run->n, earth[1], earth[2],
+                                                       earth[3], &res->rmax);
+        gi::disk_kernel<<<blocks, 256, 0, s>>>(P, reinterpret_cast<const float4 *>(vel), scope,
+                                               run->offset, run->n, earth[1], earth[2], earth[3],
+                                               earth[4], earth[5], earth[6], G * earth[0], &res->rmax,
+                                               res->counts);
+        if ((e = cudaGetLastError()) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(&host, res, sizeof host, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            break;
+    } while (false);
+    const cudaError_t ef = cudaFreeAsync(res, s);
+    if (e == cudaSuccess) e = ef;
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "gi_find_disk");
+    double r = 0.0;
+    std::memcpy(&r, &host.rmax, sizeof r);
+    out->earth_radius = r + 0.5;
+    out->n_disk = host.counts[0];
+    out->n_bound_inside = host.counts[1];
+    out->n_unbound = host.counts[2];
+    return GI_OK;
+}

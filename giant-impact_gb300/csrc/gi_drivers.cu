@@ -6,6 +6,7 @@
 // this library's fused force + kick-drift (gi_step), so a run directory
 // made by either implementation can be continued by the other.
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -295,6 +296,8 @@ extern "C" int gi_impact_add_time(int device, const char *info_dir, const char *
     const double additional = s.additional_time_days * 24.0 * 60.0 * 60.0 / b.unit_time;
     double run_time = (double)t_file;
     const double total_time = run_time + additional;
+    if (!std::isfinite(total_time) || !(s.dt > 0.0))
+        return fail(GI_ERR_PARAMS, "setup: AdditionalTime and Dt must be finite, Dt positive");
     const gi_run run{0, n, nfe, 0, mc.Dt, mc.DtOverMassFe, mc.DtOverMassSi, 0.0f};
 
     DeviceRun d;
@@ -308,6 +311,7 @@ extern "C" int gi_impact_add_time(int device, const char *info_dir, const char *
     // steps, stop after the step at which TotalRunTime < RunTime.  Steps
     // between two events run as one gi_step call.
     for (;;) {
+        if (steps >= 2000000000LL) return fail(GI_ERR_PARAMS, "add time: more than 2e9 steps");
         ++steps;
         ++pending;
         run_time += s.dt;
@@ -358,6 +362,12 @@ extern "C" int gi_impact_add_time(int device, const char *info_dir, const char *
             return st;
     path = join(impact_dir, "runStatsFile");
     if (int st = gi_write_run_stats(path.c_str(), &b, run_time, &em, S)) return file_fail(st, path);
+    // the disk (not in the reference's statistics file; reported to the caller)
+    gi_disk_info disk;
+    double disk_stats[15];
+    if (int st = gi_find_disk(d.ctx, d.pos, d.vel, &run, &p, d.scope, &disk, nullptr)) return st;
+    if (int st = gi_diag_fp64(d.ctx, d.pos, d.vel, d.scope, 4, &run, &p, disk_stats, nullptr))
+        return st;
     path = join(info.c_str(), "viewCenteringInfo");
     if (int st = gi_write_view_centering(path.c_str(), view)) return file_fail(st, path);
     if (report) {
@@ -368,6 +378,8 @@ extern "C" int gi_impact_add_time(int device, const char *info_dir, const char *
         report->end_time = run_time;
         report->seconds = secs;
         report->earth_moon = em;
+        report->disk = disk;
+        std::memcpy(report->disk_stats, disk_stats, sizeof disk_stats);
     }
     return GI_OK;
 }

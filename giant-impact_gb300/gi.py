@@ -142,10 +142,29 @@ class GenerateReport(C.Structure):
                 ("redraws", C.c_longlong), ("seconds", C.c_double)]
 
 
+class View(C.Structure):
+    _fields_ = [("eye", C.c_float * 3), ("center", C.c_float * 3), ("up", C.c_float * 3),
+                ("frustum_half", C.c_float), ("near_plane", C.c_float), ("far_plane", C.c_float),
+                ("width", C.c_int), ("height", C.c_int), ("point_size", C.c_int)]
+
+
+def view(eye, center=(0.0, 0.0, 0.0), up=(0.0, 1.0, 0.0), half=0.2, near=0.2, far=1200.0,
+         width=1000, height=1000, point_size=2) -> "View":
+    """The reference's camera by default (glFrustum(-0.2, 0.2, ...), 1000 px)."""
+    return View((C.c_float * 3)(*eye), (C.c_float * 3)(*center), (C.c_float * 3)(*up), half, near,
+                far, width, height, point_size)
+
+
+class DiskInfo(C.Structure):
+    _fields_ = [("n_disk", C.c_int), ("n_bound_inside", C.c_int), ("n_unbound", C.c_int),
+                ("earth_mass", C.c_double), ("earth_radius", C.c_double)]
+
+
 class AddTimeReport(C.Structure):
     _fields_ = [("steps", C.c_longlong), ("frames_written", C.c_longlong),
                 ("recenters", C.c_longlong), ("start_time", C.c_double),
-                ("end_time", C.c_double), ("seconds", C.c_double), ("earth_moon", EarthMoon)]
+                ("end_time", C.c_double), ("seconds", C.c_double), ("earth_moon", EarthMoon),
+                ("disk", DiskInfo), ("disk_stats", C.c_double * 15)]
 
 
 SERVER_DRY_RUN = -1
@@ -238,6 +257,13 @@ _SIGS = {
                                C.c_int),
     "gi_find_earth_moon": ([_P, _P, C.c_int, C.c_float, C.POINTER(C.c_int), _P, _P,
                             C.POINTER(EarthMoon), _P], C.c_int),
+    "gi_find_disk": ([_P, _P, _P, C.POINTER(Run), C.POINTER(PairParams), _P, C.POINTER(DiskInfo),
+                      _P], C.c_int),
+    "gi_view_basis": ([C.POINTER(View), C.POINTER(C.c_float)], C.c_int),
+    "gi_splat": ([_P, _P, C.c_int, C.POINTER(C.c_int), C.POINTER(View), _P, _P], C.c_int),
+    "gi_write_ppm": ([C.c_char_p, _P, C.c_int, C.c_int], C.c_int),
+    "gi_render_frames": ([C.c_int, C.c_char_p, C.c_char_p, C.POINTER(View), C.c_int, C.c_char_p,
+                          C.POINTER(C.c_longlong)], C.c_int),
     "gi_write_run_stats": ([C.c_char_p, C.POINTER(BodyParams), C.c_double, C.POINTER(EarthMoon),
                             C.POINTER(C.c_double)], C.c_int),
     "gi_generate_target_impactor": ([C.c_int, C.c_char_p, C.c_char_p, C.c_ulonglong,
@@ -724,6 +750,15 @@ def find_earth_moon(ctx: "Context", pos, n, touch, bounds, group=None, scope=Non
     return em
 
 
+def find_disk(ctx: "Context", pos, vel, run: Run, params: PairParams, scope, stream=0) -> DiskInfo:
+    """pos, vel, scope: device pointers; scope holds gi_find_earth_moon's labels
+    and receives 3 for disk bodies."""
+    d = DiskInfo()
+    check(lib().gi_find_disk(ctx.h, pos, vel, C.byref(run), C.byref(params), scope, C.byref(d),
+                             stream))
+    return d
+
+
 def write_run_stats(path, b: BodyParams, time, em: EarthMoon, scope_stats) -> None:
     flat = [float(x) for row in scope_stats for x in (list(row) + [0.0] * 15)[:15]]
     a = (C.c_double * 60)(*flat)
@@ -746,3 +781,33 @@ def impact_add_time(info_dir, setup_path, impact_dir, device=0) -> AddTimeReport
     check(lib().gi_impact_add_time(device, _b(info_dir), _b(setup_path), _b(impact_dir),
                                    C.byref(r)))
     return r
+
+
+# ---------------------------------------------------------------- pictures --
+
+def view_basis(v: View) -> list[float]:
+    out = (C.c_float * 12)()
+    check(lib().gi_view_basis(C.byref(v), out))
+    return list(out)
+
+
+def splat(ctx: "Context", pos, n, bounds, v: View, stream=0):
+    """pos: device pointer.  Returns a (height, width, 3) uint8 numpy image."""
+    import numpy as np
+    img = np.zeros((v.height, v.width, 3), np.uint8)
+    bd = (C.c_int * 3)(*bounds)
+    check(lib().gi_splat(ctx.h, pos, n, bd, C.byref(v), img.ctypes.data, stream))
+    return img
+
+
+def write_ppm(path, img) -> None:
+    import numpy as np
+    img = np.ascontiguousarray(img, dtype=np.uint8)
+    check(lib().gi_write_ppm(_b(path), img.ctypes.data, img.shape[1], img.shape[0]))
+
+
+def render_frames(info_dir, frames_path, v: View, out_prefix, every=1, device=0) -> int:
+    k = C.c_longlong()
+    check(lib().gi_render_frames(device, _b(info_dir), _b(frames_path), C.byref(v), every,
+                                 _b(out_prefix), C.byref(k)))
+    return k.value

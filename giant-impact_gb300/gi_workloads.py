@@ -8,6 +8,10 @@
                  impactor 0.1 x target, angle U[0, 60] deg, speed U[1.0, 1.5]
                  x escape, spin U[0, 0.8] x breakup; bodies settled together
                  in one batched damped step call.
+  precision_impact(...)  1,048,576-body target + 104,858-body impactor,
+                 each a config-1 ball scaled to the same density (radius
+                 20 (N / 8192)^(1/3) D), not settled, spun, placed and
+                 moving as in impact().
   impact(...)    two-body impact: target (60,000) and impactor (6,000), each
                  built as a seeded ball and settled on the GPU with the damped
                  separate-body step (the reference's generate-target-impactor
@@ -185,3 +189,19 @@ def sweep(gi, torch, nruns=64, seed=4, settle_steps=100, nmin=4096, nmax=131072,
         out_runs.append(run_desc(gi, off, nt + ni, nfe))
         off += nt + ni
     return np.concatenate(out_p), np.concatenate(out_v), out_runs, specs
+
+
+N3_TARGET, N3_IMPACTOR = 1_048_576, 104_858
+
+
+def precision_impact(gi, seed=3, n_t=N3_TARGET, n_i=N3_IMPACTOR):
+    """The large-N impact state (returns pos, vel, nfe in [Fe1, Fe2, Si1, Si2]
+    order): two uniform balls at the config-1 density, spun at 0.5 of
+    breakup, 45 degrees, 1.2 x the mutual escape speed."""
+    m = MATERIAL
+    rt = 20.0 * (n_t / 8192.0) ** (1.0 / 3.0)
+    ri = 20.0 * (n_i / 8192.0) ** (1.0 / 3.0)
+    pt, vt, fet = gi.ic_uniform_ball(seed, n_t, rt, 0.3, m["mass_fe"], m["mass_si"], 0.0, 1.0)
+    pi, vi, fei = gi.ic_uniform_ball(seed + 1000, n_i, ri, 0.3, m["mass_fe"], m["mass_si"], 2.0,
+                                     3.0)
+    return spin_and_place(np.concatenate([pt, pi]), np.concatenate([vt, vi]), n_t, n_i, fet, fei)

@@ -298,7 +298,8 @@ int gi_graph_destroy(gi_graph *graph);
 /* FP64 diagnostics of one run (synchronous: returns with out filled).
  * label (device, one byte per body of the whole array, may be NULL)
  * selects scope: 0 = all, 1 = label 1 or 2 (Earth + Moon), 2 = label 1
- * (Earth), 3 = label 2 (Moon)  (impactBasicFunctions.h:219-652).
+ * (Earth), 3 = label 2 (Moon)  (impactBasicFunctions.h:219-652), 4 = label 3
+ * (the disk of gi_find_disk).
  * out[0..14] = mass, com xyz, com velocity xyz, angular momentum about the
  * com relative to the com velocity xyz, kinetic energy, momentum xyz,
  * body count. */
@@ -609,11 +610,68 @@ typedef struct gi_earth_moon {
 int gi_find_earth_moon(gi_ctx *ctx, const float *pos, int n, float touch, const int bounds[3],
                        int *group, unsigned char *scope, gi_earth_moon *out, void *stream);
 
+/* The disk: bodies in neither the Earth nor the Moon that are bound to the
+ * Earth -- specific orbital energy v^2/2 - G M_E / r < 0 relative to the
+ * Earth's centre of mass and velocity -- and whose equivalent circular orbit
+ * r_eq = h^2 / (G M_E) (h = |r x v|) lies outside the Earth's radius R_E, the
+ * largest distance of an Earth element from the Earth's centre of mass plus
+ * D/2.  The reference defines no disk; this is the usual definition of
+ * giant-impact analyses.  Needs the scope array of gi_find_earth_moon; marks
+ * disk bodies 3 in it (gi_diag_fp64 scope 4).  G is read from the pair
+ * table (GMassSiSi / MassSi^2).  Synchronous; FP64. */
+typedef struct gi_disk_info {
+    int n_disk;            /* bound, r_eq > R_E                             */
+    int n_bound_inside;    /* bound, r_eq <= R_E: falls back onto the Earth */
+    int n_unbound;         /* escaping                                      */
+    double earth_mass, earth_radius;
+} gi_disk_info;
+
+int gi_find_disk(gi_ctx *ctx, const float *pos, const float *vel, const gi_run *run,
+                 const gi_pair_params *params, unsigned char *scope, gi_disk_info *out,
+                 void *stream);
+
 /* runStatsFile (recordFinalImpactStat, impactBasicFunctions.h:883-1072):
  * scope_stats[s] = gi_diag_fp64's out[0..9] for scope s = 0 (all),
  * 1 (Earth + Moon), 2 (Earth), 3 (Moon); time in code units. */
 int gi_write_run_stats(const char *path, const gi_body_params *b, double time,
                        const gi_earth_moon *em, const double scope_stats[4][15]);
+
+/* ------------------------------------------------------------------------ */
+/* Headless pictures (the reference's GL point drawing, without GL)         */
+/* ------------------------------------------------------------------------ */
+
+/* Camera of gluLookAt(eye, center, up) + glFrustum(-half, half, -half,
+ * half, near, far) (impactAddTime.cu:535-538; the reference uses eye =
+ * (0, 0, 10 R_Earth), center 0, up (0, 1, 0), half 0.2, near 0.2, far 1200,
+ * 1000 x 1000 pixels, 2-pixel points). */
+typedef struct gi_view {
+    float eye[3], center[3], up[3];
+    float frustum_half, near_plane, far_plane;
+    int width, height, point_size;
+} gi_view;
+
+/* The view's orthonormal eye basis as the splat uses it (FP32):
+ * out = [s xyz, u xyz, f xyz, eye xyz]. */
+int gi_view_basis(const gi_view *view, float out[12]);
+
+/* Splat n elements (device float4 positions) into rgb (HOST, width x height
+ * x 3 bytes, top row first): each element a point_size square coloured by
+ * origin and material (Fe body 1 yellow, Fe body 2 red, Si body 1 and 2
+ * browns, commonSetup.h:125-128; classes by index: < bounds[0], < bounds[1],
+ * < bounds[2], rest), nearest element wins, black background.
+ * Replaces drawPictureNormal's GL_POINTS (impactBasicFunctions.h:666-697).
+ * Synchronous. */
+int gi_splat(gi_ctx *ctx, const float *pos, int n, const int bounds[3], const gi_view *view,
+             unsigned char *rgb, void *stream);
+
+/* Binary PPM (P6) of an rgb image. */
+int gi_write_ppm(const char *path, const unsigned char *rgb, int width, int height);
+
+/* The viewer's playback without a window (impactViewer.cu): renders every
+ * `every`-th frame of an impactPosVel file to <out_prefix><frame>.ppm.
+ * *written (may be NULL) = images written. */
+int gi_render_frames(int device, const char *info_dir, const char *frames_path,
+                     const gi_view *view, int every, const char *out_prefix, long long *written);
 
 /* ------------------------------------------------------------------------ */
 /* Headless drivers (the reference programs without the viewer)            */
@@ -647,6 +705,8 @@ typedef struct gi_add_time_report {
     double start_time, end_time;   /* code units                             */
     double seconds;                /* wall time of the step loop             */
     gi_earth_moon earth_moon;      /* groups of the final state              */
+    gi_disk_info disk;             /* disk of the final state                */
+    double disk_stats[15];         /* gi_diag_fp64 of the disk (scope 4)     */
 } gi_add_time_report;
 
 /* impactAddTime without the window (impactAddTime.cu:396-579): resumes from

@@ -399,6 +399,7 @@ static inline int in_scope(const unsigned char *label, size_t i, int scope)
     if (scope == 1) return l == 1 || l == 2;
     if (scope == 2) return l == 1;
     if (scope == 3) return l == 2;
+    if (scope == 4) return l == 3;
     return 0;
 }
 

@@ -105,6 +105,81 @@ def test_groups_edge_cases(gi, torch_cuda):
     ctx.close()
 
 
+def test_disk_classification(gi, torch_cuda):
+    """An Earth clump, a Moon clump and test bodies on circular orbits
+    (disk), on radial infall (bound, inside) and escaping (unbound)."""
+    torch = torch_cuda
+    p = gi.params_from_material(1.0, 1.0, 1.0, 0.4, 5.0, 1.5, 0.02, 0.01, 0.002, 0.001)
+    earth = clumps(11, [8000], spacing=1.2)[:, :3].astype(np.float64)
+    earth -= earth.mean(0)
+    moon = clumps(12, [500], spacing=1.2)[:, :3].astype(np.float64) + np.array([400.0, 0, 0])
+    M = 8000 * 0.4  # all Si
+    R = np.linalg.norm(earth, axis=1).max() + 0.5
+    rng = np.random.default_rng(13)
+    extra, kinds = [], []
+    for kind, k in (("disk", 300), ("inside", 200), ("unbound", 100)):
+        for _ in range(k):
+            th, z = rng.uniform(0, 2 * np.pi), rng.uniform(-0.2, 0.2)
+            r = rng.uniform(2.0, 6.0) * R
+            x = np.array([r * np.cos(th), r * np.sin(th), z])
+            vc = np.sqrt(M / r)
+            if kind == "disk":
+                v = vc * np.array([-np.sin(th), np.cos(th), 0.0])
+            elif kind == "inside":
+                v = -0.3 * vc * x / r
+            else:
+                v = 2.0 * vc * x / r
+            extra.append((x, v))
+            kinds.append(kind)
+    n = len(earth) + len(moon) + len(extra)
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    pos[:len(earth), :3] = earth
+    pos[len(earth):len(earth) + len(moon), :3] = moon
+    for k, (x, v) in enumerate(extra):
+        pos[len(earth) + len(moon) + k, :3] = x
+        vel[len(earth) + len(moon) + k, :3] = v
+    vel[:, 3] = 0.4
+    # keep the test bodies apart from one another (no accidental groups)
+    ctx = gi.Context(0)
+    dp, dv = _dev(torch, pos), _dev(torch, vel)
+    scope = torch.zeros(n, dtype=torch.uint8, device="cuda")
+    em = gi.find_earth_moon(ctx, dp.data_ptr(), n, 1.5, [0, 0, 0], None, scope.data_ptr())
+    assert em.n_earth == 8000 and em.n_moon == 500
+    run = gi.Run(0, n, 0, 0, 0, 0, 0, 0)
+    d = gi.find_disk(ctx, dp.data_ptr(), dv.data_ptr(), run, p, scope.data_ptr())
+    assert abs(d.earth_mass - M) < 1e-6 * M
+    # FP64 classification of the same bodies
+    sc = scope.cpu().numpy()
+    c = ctx.diag(dp.data_ptr(), dv.data_ptr(), run, p, label=scope.data_ptr(), scope=2)
+    com, vcom = np.array(c[1:4]), np.array(c[4:7])
+    want = {"disk": 0, "inside": 0, "unbound": 0}
+    for k in range(len(extra)):
+        i = len(earth) + len(moon) + k
+        if sc[i] in (1, 2):
+            continue
+        r = pos[i, :3].astype(np.float64) - com
+        v = vel[i, :3].astype(np.float64) - vcom
+        eps = 0.5 * v @ v - M / np.linalg.norm(r)
+        req = np.sum(np.cross(r, v) ** 2) / M
+        got = sc[i]
+        if eps < 0 and req > d.earth_radius:
+            want["disk"] += 1
+            assert got == 3
+        elif eps < 0:
+            want["inside"] += 1
+            assert got == 0
+        else:
+            want["unbound"] += 1
+            assert got == 0
+    assert (d.n_disk, d.n_bound_inside, d.n_unbound) == (want["disk"], want["inside"],
+                                                        want["unbound"])
+    assert d.n_disk > 250 and d.n_unbound > 80
+    disk = ctx.diag(dp.data_ptr(), dv.data_ptr(), run, p, label=scope.data_ptr(), scope=4)
+    assert disk[14] == d.n_disk and abs(disk[0] - 0.4 * d.n_disk) < 1e-9
+    ctx.close()
+
+
 # ---------------------------------------------------------------- drivers --
 
 SHORT_GENERATING = (SETUP_GENERATING.replace("DampTime = 2.0", "DampTime = 0.2")
@@ -257,6 +332,7 @@ def test_impact_initialize_and_add_time(gi, orc, torch_cuda, tmp_path):
     em = rep.earth_moon
     assert em.earth_label == ref["earth"] and em.n_earth == ref["n_earth"]
     assert em.n_moon == ref["n_moon"] and list(em.earth_counts) == ref["earth_counts"]
+    assert rep.disk.earth_mass > 0 and rep.disk_stats[14] == rep.disk.n_disk
     text = (impact / "runStatsFile").read_text()
     assert "The mass of Earth" in text and "Angular momentum of the entire system" in text
     # a second call resumes from the last frame written
