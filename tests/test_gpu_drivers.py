@@ -176,7 +176,7 @@ def test_disk_classification(gi, torch_cuda):
                                                         want["unbound"])
     assert d.n_disk > 250 and d.n_unbound > 80
     disk = ctx.diag(dp.data_ptr(), dv.data_ptr(), run, p, label=scope.data_ptr(), scope=4)
-    assert disk[14] == d.n_disk and abs(disk[0] - 0.4 * d.n_disk) < 1e-9
+    assert disk[14] == d.n_disk and abs(disk[0] - float(np.float32(0.4)) * d.n_disk) < 1e-9
     ctx.close()
 
 
