@@ -71,6 +71,8 @@ def args_parse():
     ap.add_argument("--serve-rate", type=float, default=2.0)
     ap.add_argument("--advance", type=int, default=0,
                     help="untimed steps before timing (times the impact's contact phase)")
+    ap.add_argument("--dense-min", type=int, default=0,
+                    help="contact pass: bucket size for the tiled path (0 = library default)")
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--large-steps", type=int, default=4)
     ap.add_argument("--study", choices=["drift", "precision"], default=None,
@@ -567,9 +569,10 @@ def study_drift(a):
         extra.append((k, list(P), list(Lc)))
     out["ours"] = dict(_drift(log), ms_per_step=ms / steps, **_pl(extra))
     # the reference's kernels: reference units (m_Si = 1), N padded to 256
-    ref = orc.ref_lib()
+    ref = None if a.no_ref_gpu else orc.ref_lib()
     if ref is None:
-        out["reference"] = {"unavailable": "reference kernels not built"}
+        out["reference"] = {"unavailable": "skipped (--no-ref-gpu)" if a.no_ref_gpu
+                            else "reference kernels not built"}
     else:
         mu = p.MassSi
         rp = gi.params_from_material(1.0, 1.0, p.MassFe / mu, 1.0, 5.0 / mu**2, 1.5 / mu**2, 0.02,
@@ -712,7 +715,7 @@ def run_ours(a):
     wl = _load("gi_workloads", os.path.join(PKG, "gi_workloads.py"))
     import oracle as orc
 
-    ctx = gi.Context(local)
+    ctx = gi.Context(local, dense_min=a.dense_min)
     pos, vel, nfe = make_workload(gi, torch, wl, 2 + rank, a.settle_steps)
     n = len(pos)
     p = wl.params(gi)

@@ -252,7 +252,7 @@ struct StreamScratch {
 struct gi_ctx {
     int device = 0;
     int sm_count = 0;
-    gi_options opt{GI_SEP_REF_INT, GI_ACCUM_KAHAN};
+    gi_options opt{GI_SEP_REF_INT, GI_ACCUM_KAHAN, 0};
     bool forced = false;
     gi_tuning forced_tuning{0, 0};
     // Tuned i-bodies per thread per N bucket (floor(log2 n)); 0 = default.
@@ -341,6 +341,7 @@ extern "C" int gi_ctx_set_options(gi_ctx *c, const gi_options *o)
         return fail(GI_ERR_INVALID_ARG, "sep_test %d", o->sep_test);
     if (o->accum < GI_ACCUM_KAHAN || o->accum > GI_ACCUM_FP64)
         return fail(GI_ERR_INVALID_ARG, "accum %d", o->accum);
+    if (o->dense_min < 0) return fail(GI_ERR_INVALID_ARG, "dense_min %d", o->dense_min);
     c->opt = *o;
     return GI_OK;
 }
@@ -494,6 +495,7 @@ static int make_plan(const gi_ctx *c, const gi_run *runs, int nruns,
         LaunchTable t;
         std::memset(&t, 0, sizeof t);
         t.sep_test = c->opt.sep_test;
+        t.dense_min = c->opt.dense_min > 0 ? c->opt.dense_min : 64;
         const int p = ipt[order[k]];
         long long items = 0, tick = 0, part = 0, nb = 0;
         while (k < order.size() && ipt[order[k]] == p && t.nruns < GI_MAX_RUNS) {

@@ -19,6 +19,18 @@
 //      bodies landed in buckets or lanes found them, and the result is
 //      bit-reproducible.
 // The all-pairs epilogue adds the correction before its single rounding.
+//
+// Dense buckets (at least gi_options.dense_min bodies, 64 by default, e.g.
+// an interpenetrating collision remnant with thousands of contacts per
+// body) whose bodies all share one cell go through a tiled path instead: a
+// work item is (bucket, chunk of 128 of its bodies, one neighbour bucket);
+// its CTA stages that neighbour bucket in shared memory 128 bodies at a
+// time, each thread filters the tile into a hit list and evaluates the
+// contact law on the hits only, and the item's sums are added to the
+// body's correction with 64-bit integer atomics.  The candidate set, the
+// pair law and the fixed-point terms are those of the warp path and
+// integer addition is exact, so the corrections are bit-identical
+// whichever path a body takes.
 #include <algorithm>
 
 #include "gi_force_impl.cuh"
@@ -145,7 +157,9 @@ __device__ __forceinline__ float contact_coef(const PairDev &P, int sep_test, in
         if (sep) K = (r2 >= P.Tmid[test]) ? P.KRmid[test] : P.KRin[test];
     }
     const float mag = contact_mag(G, K, r2);
-    const float invr = __fdiv_rn(1.0f, __fsqrt_rn(r2));
+    // 1 / r: MUFU rsqrt and one Newton-Raphson step (about 1 ulp)
+    float invr = rsqrt_mufu(r2);
+    invr = invr * __fmaf_rn(-0.5f * r2 * invr, invr, 1.5f);
     const float ri = rsqrt_mufu(fmaxf(r2, 1.0f));
     const float s_far = (ri * ri) * ri;
     const float gmi = (i < sw) ? P.gm_fe : P.gm_si;
@@ -153,22 +167,37 @@ __device__ __forceinline__ float contact_coef(const PairDev &P, int sep_test, in
     return __fmaf_rn(mag, invr, -(gmi * gmj) * s_far);
 }
 
-// One warp per body.  Lanes 0..26 look up the 27 neighbour buckets at once
-// (one memory round trip; a bucket that two neighbour cells share is kept
-// once), a warp scan lays their bodies end to end, and the warp then walks
-// that list 32 candidates at a time.
-__global__ void __launch_bounds__(256)
-contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
-               const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
-               unsigned int mask, long long *__restrict__ delta,
-               const __grid_constant__ LaunchTable tab)
+// Buckets of at least tab.dense_min bodies (64 unless set) whose bodies
+// share one cell take the tiled path; at least kDenseFloor, which bounds
+// the item count.  Bucket state bits: 1 = mixed cells (stays on the warp
+// path), 2 = tiled.
+constexpr unsigned int kDenseFloor = 32;
+constexpr unsigned int kMixed = 1u, kTiled = 2u;
+
+// Copy of a pair table into shared memory by the first threads of the CTA,
+// so that lanes indexing it by pair class read banks rather than serialise
+// on the constant cache.
+__device__ __forceinline__ void stage_pairs(PairDev &dst, const PairDev &src)
 {
-    const RunDev &R = tab.runs[blockIdx.y];
-    const PairDev &P = tab.params[R.param];
-    const int lane = threadIdx.x & 31;
-    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (k >= R.n) return;  // whole warp leaves together
-    const int i = R.offset + k;
+    static_assert(sizeof(PairDev) % 4 == 0, "PairDev is copied word by word");
+    constexpr int kWords = (int)(sizeof(PairDev) / 4);
+    if ((int)threadIdx.x < kWords)
+        reinterpret_cast<unsigned int *>(&dst)[threadIdx.x] =
+            reinterpret_cast<const unsigned int *>(&src)[threadIdx.x];
+}
+
+// Contact correction of body i (run r) by one warp.  Lanes 0..26 look up
+// the 27 neighbour buckets at once (one memory round trip; a bucket that
+// two neighbour cells share is kept once), a warp scan lays their bodies
+// end to end, and the warp then walks that list 32 candidates at a time.
+__device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos,
+                                                  const float4 *__restrict__ vel,
+                                                  const unsigned int *__restrict__ cursor,
+                                                  const int *__restrict__ sorted, unsigned int mask,
+                                                  long long *__restrict__ delta, const RunDev &R,
+                                                  const PairDev &P, int sep_test, int r, int i,
+                                                  int lane)
+{
     const int rbeg = R.offset, rend = R.offset + R.n, sw = R.offset + R.nfe;
     const float4 pi = __ldg(&pos[i]);
     const int cx = cell_of(pi.x), cy = cell_of(pi.y), cz = cell_of(pi.z);
@@ -176,7 +205,7 @@ contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
     unsigned int b = 0xffffffffu, beg = 0u, cnt = 0u;
     if (lane < 27) {
         const int ox = lane % 3 - 1, oy = (lane / 3) % 3 - 1, oz = lane / 9 - 1;
-        b = bucket_of(blockIdx.y, cx + ox, cy + oy, cz + oz, mask);
+        b = bucket_of(r, cx + ox, cy + oy, cz + oz, mask);
     }
     const unsigned int same = __match_any_sync(0xffffffffu, b);
     const bool first = (same & ((1u << lane) - 1u)) == 0u;
@@ -218,7 +247,7 @@ contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
         if (!(r2 < 1.0f)) continue;
         if (!have_vi) { vi = __ldg(&vel[i]); have_vi = true; }
         const float4 vj = __ldg(&vel[j]);
-        const float c = contact_coef(P, tab.sep_test, i, j, sw, dx, dy, dz, r2, vi, vj) * inv_unit;
+        const float c = contact_coef(P, sep_test, i, j, sw, dx, dy, dz, r2, vi, vj) * inv_unit;
         ax += __float2ll_rn(c * dx);
         ay += __float2ll_rn(c * dy);
         az += __float2ll_rn(c * dz);
@@ -236,6 +265,201 @@ contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
     }
 }
 
+__device__ __forceinline__ unsigned int bucket_size(const unsigned int *__restrict__ cursor,
+                                                    unsigned int b)
+{
+    return __ldg(&cursor[b]) - (b ? __ldg(&cursor[b - 1]) : 0u);
+}
+
+// One warp per body of the run blockIdx.y; bodies of tiled buckets are left
+// to contact_tile_kernel.
+__global__ void __launch_bounds__(256)
+contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+               const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
+               const unsigned int *__restrict__ keys, const unsigned int *__restrict__ state,
+               unsigned int mask, long long *__restrict__ delta,
+               const __grid_constant__ LaunchTable tab)
+{
+    __shared__ PairDev sP;
+    const RunDev &R = tab.runs[blockIdx.y];
+    stage_pairs(sP, tab.params[R.param]);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (k >= R.n) return;  // whole warp leaves together
+    const int i = R.offset + k;
+    if (state[__ldg(&keys[i])] & kTiled) return;
+    contact_body_warp(pos, vel, cursor, sorted, mask, delta, R, sP, tab.sep_test, blockIdx.y, i,
+                      lane);
+}
+
+// Pass 1, one thread per body of the run blockIdx.y: for bodies of dense
+// buckets, clear the correction (the tiled path adds into it) and mark the
+// bucket mixed when the body's cell or run differs from the bucket's first
+// body.
+__global__ void __launch_bounds__(256)
+dense_check_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
+                   const unsigned int *__restrict__ keys, const unsigned int *__restrict__ cursor,
+                   const int *__restrict__ sorted, unsigned int dmin, unsigned int *state,
+                   long long *__restrict__ delta)
+{
+    const RunDev &R = tab.runs[blockIdx.y];
+    dmin = max(dmin, kDenseFloor);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < R.n; k += gridDim.x * blockDim.x) {
+        const int i = R.offset + k;
+        const unsigned int b = keys[i];
+        if (bucket_size(cursor, b) < dmin) continue;
+        delta[3 * (size_t)i + 0] = 0;
+        delta[3 * (size_t)i + 1] = 0;
+        delta[3 * (size_t)i + 2] = 0;
+        const int j0 = sorted[b ? cursor[b - 1] : 0u];
+        if (j0 == i) continue;
+        bool mixed = j0 < R.offset || j0 >= R.offset + R.n;
+        if (!mixed) {
+            const float4 p = pos[i], q = pos[j0];
+            mixed = cell_of(p.x) != cell_of(q.x) || cell_of(p.y) != cell_of(q.y) ||
+                    cell_of(p.z) != cell_of(q.z);
+        }
+        if (mixed) atomicOr(&state[b], kMixed);
+    }
+}
+
+__device__ __forceinline__ int run_of_body(const LaunchTable &tab, int i)
+{
+    for (int q = 0; q < tab.nruns; ++q)
+        if (i >= tab.runs[q].offset && i < tab.runs[q].offset + tab.runs[q].n) return q;
+    return 0;
+}
+
+// Item = bucket (27 bits) << 37 | chunk of 128 bodies (32 bits) << 5 |
+// neighbour offset (0..26).
+__device__ __forceinline__ unsigned long long make_item(unsigned int b, unsigned int c, int q)
+{
+    return ((unsigned long long)b << 37) | ((unsigned long long)c << 5) | (unsigned long long)q;
+}
+
+// Pass 2, one thread per bucket: a dense bucket of one cell becomes tiled
+// and gets an item per (chunk, distinct non-empty neighbour bucket).
+__global__ void __launch_bounds__(256)
+dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
+                   const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
+                   unsigned int m, unsigned int mask, unsigned int dmin, unsigned int *state,
+                   unsigned long long *__restrict__ items, unsigned int *__restrict__ nitems)
+{
+    dmin = max(dmin, kDenseFloor);
+    for (unsigned int b = blockIdx.x * blockDim.x + threadIdx.x; b < m; b += gridDim.x * blockDim.x) {
+        const unsigned int cnt = bucket_size(cursor, b);
+        if (cnt < dmin || (state[b] & kMixed)) continue;
+        state[b] = kTiled;
+        const int j0 = sorted[b ? cursor[b - 1] : 0u];
+        const int r = run_of_body(tab, j0);
+        const float4 p = pos[j0];
+        const int cx = cell_of(p.x), cy = cell_of(p.y), cz = cell_of(p.z);
+        unsigned int nb[27];
+        unsigned int uniq = 0;  // bit q: offset q is the first to reach its bucket
+        for (int q = 0; q < 27; ++q) {
+            nb[q] = bucket_of(r, cx + q % 3 - 1, cy + (q / 3) % 3 - 1, cz + q / 9 - 1, mask);
+            bool dup = false;
+            for (int u = 0; u < q; ++u) dup |= nb[u] == nb[q];
+            if (!dup && bucket_size(cursor, nb[q]) > 0) uniq |= 1u << q;
+        }
+        const unsigned int nch = (cnt + 127u) / 128u;
+        const unsigned int nq = __popc(uniq);
+        unsigned int at = atomicAdd(nitems, nch * nq);
+        for (unsigned int c = 0; c < nch; ++c)
+            for (int q = 0; q < 27; ++q)
+                if (uniq & (1u << q)) items[at++] = make_item(b, c, q);
+    }
+}
+
+// Grid-stride over the items.  For an item the CTA holds up to 128 bodies
+// of the bucket (one per thread, all in one cell), stages the neighbour
+// bucket in shared memory 128 bodies at a time, and each thread collects
+// the tile slots within r2 < 1 of its body before evaluating the contact
+// law on those alone.
+__global__ void __launch_bounds__(128)
+contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                    const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
+                    unsigned int mask, long long *__restrict__ delta,
+                    const __grid_constant__ LaunchTable tab,
+                    const unsigned long long *__restrict__ items,
+                    const unsigned int *__restrict__ nitems)
+{
+    constexpr int kStride = 132;  // bytes per hit list row: rows start in distinct banks
+    __shared__ float4 sp[128];
+    __shared__ float4 sv[128];
+    __shared__ int sj[128];
+    __shared__ unsigned char hits[128 * kStride];
+    __shared__ PairDev sP;
+    const unsigned int total = *nitems;
+    const int t = threadIdx.x;
+    unsigned char *my = hits + t * kStride;
+    for (unsigned int w = blockIdx.x; w < total; w += gridDim.x) {
+        const unsigned long long it = items[w];
+        const unsigned int b = (unsigned int)(it >> 37);
+        const unsigned int chunk = (unsigned int)((it >> 5) & 0xffffffffull);
+        const int q = (int)(it & 31ull);
+        const unsigned int bbeg = b ? cursor[b - 1] : 0u, bend = cursor[b];
+        const unsigned int s0 = bbeg + 128u * chunk;
+        const bool valid = s0 + (unsigned int)t < bend;
+        const int j0 = sorted[s0];  // every item's chunk holds at least one body
+        const int run = run_of_body(tab, j0);
+        const RunDev &R = tab.runs[run];
+        __syncthreads();  // every thread is done with the previous item's table
+        stage_pairs(sP, tab.params[R.param]);
+        const int rbeg = R.offset, rend = R.offset + R.n, sw = R.offset + R.nfe;
+        const float inv_unit = (float)(1.0 / tab.params[R.param].fx_unit);
+        const float4 p0 = pos[j0];
+        const unsigned int nb = bucket_of(run, cell_of(p0.x) + q % 3 - 1,
+                                          cell_of(p0.y) + (q / 3) % 3 - 1, cell_of(p0.z) + q / 9 - 1,
+                                          mask);
+        const unsigned int nbeg = nb ? cursor[nb - 1] : 0u, nend = cursor[nb];
+        const int i = valid ? sorted[s0 + t] : -1;
+        const float4 pi = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 vi = valid ? vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        long long ax = 0, ay = 0, az = 0;
+        for (unsigned int base = nbeg; base < nend; base += 128u) {
+            __syncthreads();  // the previous tile is consumed; sP is written
+            const unsigned int u = base + (unsigned int)t;
+            if (u < nend) {
+                const int j = sorted[u];
+                sj[t] = j;
+                sp[t] = pos[j];
+                sv[t] = vel[j];
+            }
+            __syncthreads();
+            if (!valid) continue;
+            const int cnt = (int)min(128u, nend - base);
+            int nh = 0;
+            for (int k = 0; k < cnt; ++k) {
+                const float4 pj = sp[k];
+                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+                if (r2 < 1.0f) my[nh++] = (unsigned char)k;
+            }
+            for (int h = 0; h < nh; ++h) {
+                const int k = my[h];
+                const int j = sj[k];
+                if (j == i || j < rbeg || j >= rend) continue;
+                const float4 pj = sp[k];
+                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+                const float c =
+                    contact_coef(sP, tab.sep_test, i, j, sw, dx, dy, dz, r2, vi, sv[k]) * inv_unit;
+                ax += __float2ll_rn(c * dx);
+                ay += __float2ll_rn(c * dy);
+                az += __float2ll_rn(c * dz);
+            }
+        }
+        if (valid && (ax | ay | az)) {
+            unsigned long long *d = reinterpret_cast<unsigned long long *>(delta + 3 * (size_t)i);
+            atomicAdd(d + 0, (unsigned long long)ax);
+            atomicAdd(d + 1, (unsigned long long)ay);
+            atomicAdd(d + 2, (unsigned long long)az);
+        }
+    }
+}
+
 }  // namespace gi
 
 // Buckets of the grid for `bodies` bodies: a power of two >= 2 * bodies.
@@ -246,11 +470,21 @@ unsigned int gi_grid_buckets(long long bodies)
     return (unsigned int)m;
 }
 
-// keys + sorted: `bodies` each (indexed by global body index / slot); cursor:
-// buckets; block sums: 8192.
+// Tiled-path work items: at most 27 per chunk of 128 bodies of a dense
+// bucket, and a dense bucket holds at least kDenseFloor bodies, so at most
+// 27 (bodies / 128 + bodies / kDenseFloor + 2).
+static size_t dense_item_capacity(long long bodies)
+{
+    return 27 * ((size_t)bodies / 128 + (size_t)bodies / gi::kDenseFloor + 2);
+}
+
+// keys + sorted: `bodies` each (indexed by global body index / slot); cursor
+// and bucket state: one word per bucket each; block sums: 8192; item count
+// (2 words) and items (2 words each).
 size_t gi_grid_words(long long max_end, long long bodies)
 {
-    return 2 * (size_t)max_end + gi_grid_buckets(bodies) + 8192;
+    return 2 * (size_t)max_end + 2 * (size_t)gi_grid_buckets(bodies) + 8192 + 2 +
+           2 * dense_item_capacity(bodies);
 }
 
 cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, cudaStream_t s)
@@ -273,11 +507,18 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     unsigned int *keys = work;
     int *sorted = reinterpret_cast<int *>(work + max_end);
     unsigned int *cursor = work + 2 * (size_t)max_end;
-    unsigned int *sums = cursor + m;
+    unsigned int *state = cursor + m;
+    unsigned int *sums = state + m;
+    unsigned int *nitems = sums + 8192;
+    unsigned long long *items = reinterpret_cast<unsigned long long *>(nitems + 2);  // 8-byte aligned
     int maxn = 0;
     for (int r = 0; r < tab.nruns; ++r) maxn = std::max(maxn, tab.runs[r].n);
     if (maxn == 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(cursor, 0, (size_t)m * sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(state, 0, (size_t)m * sizeof(unsigned int), s);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(nitems, 0, sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
     const dim3 gk(std::min(4 * nsm, (maxn + 255) / 256), tab.nruns);
     gi::grid_keys<<<gk, 256, 0, s>>>(pos, tab, m - 1, keys, cursor);
@@ -286,7 +527,13 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     gi::scan_sums<<<1, 1024, 0, s>>>(sums, sb);
     gi::scan_add<<<sb, 1024, 0, s>>>(cursor, (int)m, sums);
     gi::grid_scatter<<<gk, 256, 0, s>>>(tab, keys, cursor, sorted);
+    const unsigned int dmin = (unsigned int)tab.dense_min;
+    gi::dense_check_kernel<<<gk, 256, 0, s>>>(pos, tab, keys, cursor, sorted, dmin, state, delta);
+    gi::dense_items_kernel<<<std::min((int)((m + 255) / 256), 4 * nsm), 256, 0, s>>>(
+        pos, tab, cursor, sorted, m, m - 1, dmin, state, items, nitems);
     const dim3 gc((maxn + 7) / 8, tab.nruns);
-    gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, cursor, sorted, m - 1, delta, tab);
+    gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, cursor, sorted, keys, state, m - 1, delta, tab);
+    gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(pos, vel, cursor, sorted, m - 1, delta, tab,
+                                                     items, nitems);
     return cudaGetLastError();
 }

@@ -56,7 +56,7 @@ struct LaunchTable {
     int nruns;
     int nitems;
     int sep_test;
-    int pad;
+    int dense_min;  // contact pass: bucket size from which the tiled kernel takes it
     RunDev runs[GI_MAX_RUNS];
     PairDev params[GI_MAX_PARAMS];
 };

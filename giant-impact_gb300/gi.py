@@ -47,7 +47,7 @@ class Run(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("sep_test", C.c_int), ("accum", C.c_int)]
+    _fields_ = [("sep_test", C.c_int), ("accum", C.c_int), ("dense_min", C.c_int)]
 
 
 class Tuning(C.Structure):
@@ -388,11 +388,11 @@ class Context:
     """Owns a gi_ctx (scratch, options, tuning) on one device."""
 
     def __init__(self, device: int = 0, sep_test: int = GI_SEP_REF_INT,
-                 accum: int = GI_ACCUM_KAHAN):
+                 accum: int = GI_ACCUM_KAHAN, dense_min: int = 0):
         h = C.c_void_p()
         check(lib().gi_ctx_create(C.byref(h), device))
         self.h = h
-        self.set_options(sep_test, accum)
+        self.set_options(sep_test, accum, dense_min)
 
     def close(self):
         if self.h:
@@ -405,8 +405,8 @@ class Context:
         except Exception:
             pass
 
-    def set_options(self, sep_test=GI_SEP_REF_INT, accum=GI_ACCUM_KAHAN):
-        o = Options(sep_test, accum)
+    def set_options(self, sep_test=GI_SEP_REF_INT, accum=GI_ACCUM_KAHAN, dense_min=0):
+        o = Options(sep_test, accum, dense_min)
         check(lib().gi_ctx_set_options(self.h, C.byref(o)))
 
     def set_tuning(self, i_per_thread=None, jchunk=0):

@@ -421,3 +421,42 @@ def test_large_n_subsample_vs_fp64(gi, orc, torch_cuda, ctx):
     print(f"N={n}: subsample rel L2 {err:.3e}")
     assert err < FORCE_TOL
     assert np.isfinite(f[:, :3]).all()
+
+
+def test_dense_contact_path_matches_sparse_path(gi, orc, torch_cuda):
+    """A collapsed remnant (cells of hundreds of bodies, thousands of contacts
+    per body) next to a sparse ball: the shared-memory tiled contact pass
+    (dense cells) and the warp-per-body pass give bit-identical forces, and
+    both stay within the force tolerance of the FP64 oracle."""
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    n_dense, n_sparse = 12000, 8000
+    rng = np.random.default_rng(23)
+    d = rng.normal(size=(n_dense, 3))
+    d = d / np.linalg.norm(d, axis=1, keepdims=True) * (rng.uniform(0, 1, size=(n_dense, 1)) ** (1 / 3)) * 4.0
+    sp, _, _ = ball_with_velocities(gi, n_sparse, 24)
+    pos = np.zeros((n_dense + n_sparse, 4), np.float32)
+    pos[:n_dense, :3] = d
+    pos[n_dense:] = sp
+    pos[n_dense:, 0] += 60.0
+    vel = np.zeros_like(pos)
+    vel[:, :3] = rng.normal(scale=2.0, size=(len(pos), 3)).astype(np.float32)
+    vel[:, 3] = 0.4
+    nfe = 1500
+    run = wl.run_desc(gi, 0, len(pos), nfe)
+    tiled = gi.Context(0, dense_min=64)
+    warp = gi.Context(0, dense_min=1 << 30)
+    ft = gpu_forces(gi, torch, tiled, pos, vel, [run], p)
+    fw = gpu_forces(gi, torch, warp, pos, vel, [run], p)
+    ft2 = gpu_forces(gi, torch, tiled, pos, vel, [run], p)
+    tiled.close()
+    warp.close()
+    assert np.isfinite(ft[:, :3]).all()
+    assert np.array_equal(ft[:, :3], fw[:, :3])
+    assert np.array_equal(ft[:, :3], ft2[:, :3])
+    idx = np.concatenate([np.arange(0, n_dense, 61), np.arange(n_dense, len(pos), 97)]).astype(np.int32)
+    f64, _ = orc.forces_fp64(pos, vel, [(0, len(pos), nfe, 0, 0, 0, 0, 0)], p, idx=idx)
+    err = rel_l2(ft[idx, :3], f64)
+    print(f"dense remnant: rel L2 vs FP64 {err:.3e}")
+    assert err < FORCE_TOL
