@@ -495,7 +495,7 @@ static int make_plan(const gi_ctx *c, const gi_run *runs, int nruns,
         LaunchTable t;
         std::memset(&t, 0, sizeof t);
         t.sep_test = c->opt.sep_test;
-        t.dense_min = c->opt.dense_min > 0 ? c->opt.dense_min : 64;
+        t.dense_min = c->opt.dense_min > 0 ? c->opt.dense_min : 256;
         const int p = ipt[order[k]];
         long long items = 0, tick = 0, part = 0, nb = 0;
         while (k < order.size() && ipt[order[k]] == p && t.nruns < GI_MAX_RUNS) {

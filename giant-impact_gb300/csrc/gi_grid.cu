@@ -20,7 +20,7 @@
 //      bit-reproducible.
 // The all-pairs epilogue adds the correction before its single rounding.
 //
-// Dense buckets (at least gi_options.dense_min bodies, 64 by default, e.g.
+// Dense buckets (at least gi_options.dense_min bodies, 256 by default, e.g.
 // an interpenetrating collision remnant with thousands of contacts per
 // body) whose bodies all share one cell go through a tiled path instead: a
 // work item is (bucket, chunk of 128 of its bodies, one neighbour bucket);
@@ -167,7 +167,7 @@ __device__ __forceinline__ float contact_coef(const PairDev &P, int sep_test, in
     return __fmaf_rn(mag, invr, -(gmi * gmj) * s_far);
 }
 
-// Buckets of at least tab.dense_min bodies (64 unless set) whose bodies
+// Buckets of at least tab.dense_min bodies (256 unless set) whose bodies
 // share one cell take the tiled path; at least kDenseFloor, which bounds
 // the item count.  Bucket state bits: 1 = mixed cells (stays on the warp
 // path), 2 = tiled.

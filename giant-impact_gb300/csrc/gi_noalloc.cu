@@ -128,7 +128,7 @@ extern "C" int gi_forces_collision_noalloc(const float *pos, const float *vel, f
     tab.nruns = 1;
     tab.nitems = d.nib * d.nsplit;
     tab.sep_test = GI_SEP_REF_INT;
-    tab.dense_min = 64;
+    tab.dense_min = 256;
 
     // Carve the static array.
     const size_t grid_bytes = align256(gi_grid_words(n, n) * sizeof(unsigned int));
