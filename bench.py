@@ -80,6 +80,8 @@ def args_parse():
     ap.add_argument("--study-steps", type=int, default=None)
     ap.add_argument("--study-every", type=int, default=100)
     ap.add_argument("--subsample", type=int, default=65536)
+    ap.add_argument("--conservative", action="store_true",
+                    help="drift study with KR = K (no dissipation): energy then measures numerics")
     return ap.parse_args()
 
 
@@ -549,10 +551,15 @@ def study_drift(a):
     ctx = gi.Context(0)
     pos, vel, nfe = make_workload(gi, torch, wl, 2, a.settle_steps)
     n = len(pos)
-    p = wl.params(gi)
+    kr = 1.0 if a.conservative else None  # KR = K: the contact law is conservative
+    m = wl.MATERIAL
+    p = wl.params(gi) if kr is None else gi.params_from_material(
+        m["G"], m["diameter"], m["mass_fe"], m["mass_si"], m["k_fe"], m["k_si"], kr, kr,
+        m["sd_fe"], m["sd_si"])
     run = wl.run_desc(gi, 0, n, nfe)
     out = {"study": "drift", "workload": "plain two-body impact, 66,000 bodies, dt 1e-3",
-           "steps": steps, "every": every}
+           "steps": steps, "every": every,
+           "material": "KR = K (conservative control)" if kr is not None else "config 2"}
     # this library: fused step, config units
     dp, dv = torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda()
     log, ms, extra = [], 0.0, []
@@ -575,8 +582,8 @@ def study_drift(a):
                             else "reference kernels not built"}
     else:
         mu = p.MassSi
-        rp = gi.params_from_material(1.0, 1.0, p.MassFe / mu, 1.0, 5.0 / mu**2, 1.5 / mu**2, 0.02,
-                                     0.01, 0.002, 0.001)
+        rp = gi.params_from_material(1.0, 1.0, p.MassFe / mu, 1.0, 5.0 / mu**2, 1.5 / mu**2,
+                                     kr or 0.02, kr or 0.01, 0.002, 0.001)
         nr = ((n + 255) // 256) * 256
         pp = np.zeros((nr, 4), np.float32)
         vv = np.zeros((nr, 4), np.float32)
