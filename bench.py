@@ -363,7 +363,9 @@ def serve_section(gi, torch, wl, a):
     a.serve_steps steps.  Continuous batching: requests are submitted to
     gi_server as they arrive (real time) and admitted by HBM budget (150 GB)
     and slots (64); every round advances all live runs a.serve_round steps in
-    one force launch per step.  Plain per-run path: the same stream served
+    one force launch per step (policy GI_SERVE_SHARE), or the runs with the
+    least remaining work until a step fills the GPU (GI_SERVE_SHORTEST).
+    Plain per-run path: the same stream served
     one run at a time (FIFO), unfused force + kick-drift per step; its
     timeline uses each run's measured GPU service time.  Latency per 1,000
     steps = (done - arrival) / (steps / 1000); service latency counts from
@@ -377,42 +379,48 @@ def serve_section(gi, torch, wl, a):
     arrivals = np.cumsum(rng.exponential(1.0 / a.serve_rate, size=R))
     arrivals -= arrivals[0]
     per_k = a.serve_steps / 1000.0
-    # ---- continuous batching
-    srv = gi.Server(p, device=torch.cuda.current_device(), budget_bytes=150 << 30, max_live_runs=64,
-                    steps_per_round=a.serve_round)
-    ids, nxt = {}, 0
-    t0 = time.perf_counter()
-    done = {}
-    while len(done) < R:
-        now = time.perf_counter() - t0
-        while nxt < R and arrivals[nxt] <= now:
-            r = runs[nxt]
-            one = gi.Run(0, r.n, r.nfe, 0, r.dt, r.dt_over_mass_fe, r.dt_over_mass_si, 0.0)
-            ids[nxt] = srv.submit(pos[r.offset:r.offset + r.n], vel[r.offset:r.offset + r.n], one,
-                                  a.serve_steps)
-            nxt += 1
-        st = srv.stats()
-        if st.live == 0 and st.queued == 0:
-            if nxt < R:
-                time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
-            continue
-        srv.round()
-        for k, rid in ids.items():
-            if k not in done:
-                info = srv.query(rid)
-                if info.state == gi.REQ_DONE:
-                    done[k] = info
-    t_end = max(i.t_done for i in done.values())
-    t_origin = min(i.t_submit for i in done.values()) - arrivals[0]
     inter = sum(r.n * (r.n - 1) for r in runs) * a.serve_steps
-    lat = [(done[k].t_done - (t_origin + arrivals[k])) / per_k for k in range(R)]
-    svc = [(done[k].t_done - done[k].t_admit) / per_k for k in range(R)]
-    batched = {"p50_s_per_1000_steps": _pct(lat, 50), "p99_s_per_1000_steps": _pct(lat, 99),
+
+    def serve(policy):
+        srv = gi.Server(p, device=torch.cuda.current_device(), budget_bytes=150 << 30,
+                        max_live_runs=64, steps_per_round=a.serve_round, policy=policy)
+        ids, nxt = {}, 0
+        t0 = time.perf_counter()
+        done = {}
+        while len(done) < R:
+            now = time.perf_counter() - t0
+            while nxt < R and arrivals[nxt] <= now:
+                r = runs[nxt]
+                one = gi.Run(0, r.n, r.nfe, 0, r.dt, r.dt_over_mass_fe, r.dt_over_mass_si, 0.0)
+                ids[nxt] = srv.submit(pos[r.offset:r.offset + r.n], vel[r.offset:r.offset + r.n],
+                                      one, a.serve_steps)
+                nxt += 1
+            st = srv.stats()
+            if st.live == 0 and st.queued == 0:
+                if nxt < R:
+                    time.sleep(max(0.0, arrivals[nxt] - (time.perf_counter() - t0)))
+                continue
+            srv.round()
+            for k, rid in ids.items():
+                if k not in done:
+                    info = srv.query(rid)
+                    if info.state == gi.REQ_DONE:
+                        done[k] = info
+        t_end = max(i.t_done for i in done.values())
+        t_origin = min(i.t_submit for i in done.values()) - arrivals[0]
+        lat = [(done[k].t_done - (t_origin + arrivals[k])) / per_k for k in range(R)]
+        svc = [(done[k].t_done - done[k].t_admit) / per_k for k in range(R)]
+        out = {"p50_s_per_1000_steps": _pct(lat, 50), "p99_s_per_1000_steps": _pct(lat, 99),
                "service_p50_s_per_1000_steps": _pct(svc, 50),
                "service_p99_s_per_1000_steps": _pct(svc, 99),
                "interactions_per_s": inter / (t_end - t_origin), "makespan_s": t_end - t_origin,
                "rounds": srv.stats().rounds}
-    srv.close()
+        srv.close()
+        return out
+
+    # ---- continuous batching, two stepping policies
+    batched = serve(gi.SERVE_SHARE)
+    shortest = serve(gi.SERVE_SHORTEST)
     # ---- plain per-run path, FIFO
     ctx = gi.Context(torch.cuda.current_device())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -444,7 +452,7 @@ def serve_section(gi, torch, wl, a):
     return {"requests": R, "steps_per_request": a.serve_steps, "arrival_rate_per_s": a.serve_rate,
             "steps_per_round": a.serve_round, "n_min": ns[0], "n_median": ns[len(ns) // 2],
             "n_max": ns[-1], "interactions": inter, "hbm_budget_gb": 150, "slots": 64,
-            "batched": batched, "plain": plain,
+            "batched": batched, "batched_shortest_first": shortest, "plain": plain,
             # interactions asked for per second of the arrival window, over what was served
             "offered_over_served": (inter / max(arrivals[-1], 1e-9)) /
                                    max(batched["interactions_per_s"], 1.0),

@@ -6,10 +6,13 @@
 //      and its device memory (two state buffers + scratch estimate) fits in
 //      the HBM budget; its bodies are copied into a contiguous range of the
 //      device pool (first-fit free list; the pool grows within the budget);
-//   2. step: every live run advances `steps_per_round` steps, all runs in
-//      one persistent force launch per step (gi_step_pingpong over the live
+//   2. step: the live runs advance `steps_per_round` steps, all stepped runs
+//      in one persistent force launch per step (gi_step_pingpong over the
 //      run table); a run whose remaining steps run out mid-round simply drops
-//      out of the next step's table;
+//      out of the next step's table.  GI_SERVE_SHARE steps every live run;
+//      GI_SERVE_SHORTEST steps the runs with the least remaining work until
+//      a step's pair interactions fill the GPU (one large run already does),
+//      so short requests finish first and the GPU stays full;
 //   3. retire: finished runs are copied to host memory and their range freed.
 // A run's result depends only on its own bodies, N and the context's tuning
 // table (the force kernel is batch-invariant), so it is the same alone and
@@ -191,22 +194,57 @@ int admit(gi_server *s)
     return GI_OK;
 }
 
+// Live runs to step next, by policy.
+std::vector<long long> select_runs(gi_server *s)
+{
+    std::vector<long long> ids;
+    for (long long id : s->live)
+        if (s->reqs[id].nsteps > s->reqs[id].steps_done) ids.push_back(id);
+    if (s->cfg.policy != GI_SERVE_SHORTEST || ids.empty()) return ids;
+    auto work = [&](long long id) {
+        const Req &q = s->reqs[id];
+        return (double)(q.nsteps - q.steps_done) * (double)q.run.n * (double)q.run.n;
+    };
+    std::stable_sort(ids.begin(), ids.end(),
+                     [&](long long a, long long b) { return work(a) < work(b); });
+    const double fill = s->cfg.fill_interactions > 0 ? (double)s->cfg.fill_interactions : 2e9;
+    double per_step = 0.0;
+    size_t k = 0;
+    while (k < ids.size() && (k == 0 || per_step < fill)) {
+        const Req &q = s->reqs[ids[k]];
+        per_step += (double)q.run.n * (double)(q.run.n - 1);
+        ++k;
+    }
+    ids.resize(k);
+    return ids;
+}
+
 int step_round(gi_server *s)
 {
     const int S = s->cfg.steps_per_round;
     for (int k = 0; k < S;) {
         std::vector<gi_run> runs;
-        std::vector<long long> ids;
+        std::vector<long long> ids = select_runs(s);
         int span = S - k;  // steps every selected run can take without dropping out
-        for (long long id : s->live) {
+        for (long long id : ids) {
             Req &q = s->reqs[id];
-            const int rem = q.nsteps - q.steps_done;
-            if (rem <= 0) continue;
-            span = std::min(span, rem);
+            span = std::min(span, q.nsteps - q.steps_done);
             gi_run r = q.run;
             r.offset = (int)q.offset;
             runs.push_back(r);
-            ids.push_back(id);
+            // a run left out of earlier steps may sit in the other state buffer
+            if (q.where != s->cur && !s->dry && q.run.n > 0) {
+                const size_t bytes = (size_t)q.run.n * 16;
+                cudaError_t e = cudaMemcpyAsync(s->pos[s->cur] + 4 * q.offset,
+                                                s->pos[q.where] + 4 * q.offset, bytes,
+                                                cudaMemcpyDeviceToDevice, s->stream);
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(s->vel[s->cur] + 4 * q.offset,
+                                        s->vel[q.where] + 4 * q.offset, bytes,
+                                        cudaMemcpyDeviceToDevice, s->stream);
+                if (e != cudaSuccess) return gi_internal_fail(GI_ERR_CUDA, "state copy failed");
+            }
+            q.where = s->cur;
         }
         if (runs.empty()) break;
         if (!s->dry) {
@@ -272,6 +310,9 @@ extern "C" int gi_server_create(int device, const gi_server_config *cfg,
     *out = nullptr;
     if (cfg->hbm_budget_bytes <= 0 || cfg->max_live_runs < 1 || cfg->steps_per_round < 1)
         return gi_internal_fail(GI_ERR_INVALID_ARG, "budget, slots and steps_per_round must be positive");
+    if ((cfg->policy != GI_SERVE_SHARE && cfg->policy != GI_SERVE_SHORTEST) ||
+        cfg->fill_interactions < 0)
+        return gi_internal_fail(GI_ERR_INVALID_ARG, "unknown policy or negative fill");
     if (nparams < 1 || nparams > GI_MAX_PARAMS)
         return gi_internal_fail(GI_ERR_BAD_SIZE, "nparams out of range");
     gi_server *s = new gi_server();

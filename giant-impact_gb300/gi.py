@@ -79,7 +79,11 @@ class MoveSeparateConsts(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_longlong), ("max_live_runs", C.c_int),
-                ("steps_per_round", C.c_int)]
+                ("steps_per_round", C.c_int), ("policy", C.c_int),
+                ("fill_interactions", C.c_longlong)]
+
+
+SERVE_SHARE, SERVE_SHORTEST = 0, 1
 
 
 class RequestInfo(C.Structure):
@@ -500,9 +504,9 @@ class Server:
     """Continuous-batching serving loop (gi_server_*)."""
 
     def __init__(self, params, device=0, budget_bytes=150 << 30, max_live_runs=64,
-                 steps_per_round=100):
+                 steps_per_round=100, policy=SERVE_SHARE, fill_interactions=0):
         pa, npar = _arr(params, PairParams)
-        cfg = ServerConfig(budget_bytes, max_live_runs, steps_per_round)
+        cfg = ServerConfig(budget_bytes, max_live_runs, steps_per_round, policy, fill_interactions)
         h = C.c_void_p()
         check(lib().gi_server_create(device, C.byref(cfg), pa, npar, C.byref(h)))
         self.h = h

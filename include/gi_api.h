@@ -345,10 +345,20 @@ int gi_measure_ffma_peak(int device, double *tflops);
 #define GI_REQ_LIVE 1
 #define GI_REQ_DONE 2
 
+/* Stepping policy of a round. */
+#define GI_SERVE_SHARE 0     /* every live run advances each round            */
+#define GI_SERVE_SHORTEST 1  /* live runs in order of least remaining work
+                                (steps left x N^2) until the per-step pair
+                                count reaches fill_interactions; the others
+                                wait (shortest remaining work first)          */
+
 typedef struct gi_server_config {
     long long hbm_budget_bytes;  /* device memory the live runs may hold */
     int max_live_runs;           /* slots */
     int steps_per_round;         /* steps per round (latency granularity) */
+    int policy;                  /* GI_SERVE_*                             */
+    long long fill_interactions; /* GI_SERVE_SHORTEST: pair interactions per
+                                    step that fill the GPU; 0 = 2e9        */
 } gi_server_config;
 
 typedef struct gi_server_request_info {

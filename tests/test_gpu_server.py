@@ -8,7 +8,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_each_result_same_alone_and_in_the_mix(gi, torch_cuda):
+@pytest.mark.parametrize("policy", [0, 1])
+def test_each_result_same_alone_and_in_the_mix(gi, torch_cuda, policy):
     torch = torch_cuda
     import gi_workloads as wl
     p = wl.params(gi)
@@ -18,13 +19,16 @@ def test_each_result_same_alone_and_in_the_mix(gi, torch_cuda):
     for k, (n, ns) in enumerate(zip(sizes, steps)):
         pos, vel, nfe = gi.ic_lattice(70 + k, n, spacing=0.999, jitter=0.004, vel_sigma=1.0)
         reqs.append((pos, vel, wl.run_desc(gi, 0, n, nfe), ns))
-    srv = gi.Server(p, device=0, budget_bytes=1 << 30, max_live_runs=3, steps_per_round=10)
+    # policy 1 with a small fill target leaves runs out of rounds, so their
+    # state must move between the two pool buffers correctly
+    srv = gi.Server(p, device=0, budget_bytes=1 << 30, max_live_runs=3, steps_per_round=10,
+                    policy=policy, fill_interactions=2_000_000)
     ids = {}
     for k, (pos, vel, r, ns) in enumerate(reqs):
         ids[k] = srv.submit(pos, vel, r, ns)
         if k % 2 == 1:
             srv.round()  # arrivals interleaved with rounds: the mix keeps changing
-    for _ in range(20):
+    for _ in range(60):
         if srv.stats().completed == len(reqs):
             break
         srv.round()

@@ -88,3 +88,39 @@ def test_bad_requests(gi, params):
         srv.submit(*bodies(10), gi.Run(0, 10, 1, 3, 0, 0, 0, 0), 5)
     with pytest.raises(gi.GIError):
         srv.submit(*bodies(10), run(gi, 10), -1)
+
+
+def test_shortest_remaining_work_first(gi, params):
+    """GI_SERVE_SHORTEST steps the live runs with the least remaining work
+    (steps left x N^2) until a step's pair count reaches the fill target;
+    the others wait.  Every run still gets exactly its steps."""
+    # fill at 1 interaction: one run per step, the cheapest first
+    srv = gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=10**9, max_live_runs=8,
+                    steps_per_round=10, policy=gi.SERVE_SHORTEST, fill_interactions=1)
+    big = srv.submit(*bodies(3000), run(gi, 3000), 20)
+    small = srv.submit(*bodies(300), run(gi, 300), 30)
+    mid = srv.submit(*bodies(1000), run(gi, 1000), 20)
+    srv.round()
+    q = {k: srv.query(i) for k, i in (("big", big), ("small", small), ("mid", mid))}
+    assert (q["small"].steps_done, q["mid"].steps_done, q["big"].steps_done) == (10, 0, 0)
+    for _ in range(2):
+        srv.round()
+    assert srv.query(small).state == gi.REQ_DONE       # 30 steps in the first 3 rounds
+    assert srv.query(mid).steps_done == 0 and srv.query(big).steps_done == 0
+    for _ in range(2):
+        srv.round()
+    assert srv.query(mid).state == gi.REQ_DONE and srv.query(big).steps_done == 0
+    for _ in range(2):
+        srv.round()
+    assert srv.query(big).state == gi.REQ_DONE
+    st = srv.stats()
+    assert st.interactions == 20 * 3000 * 2999 + 30 * 300 * 299 + 20 * 1000 * 999
+    # a fill target of the two smaller runs' pair count steps both of them together
+    srv2 = gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=10**9, max_live_runs=8,
+                     steps_per_round=10, policy=gi.SERVE_SHORTEST,
+                     fill_interactions=300 * 299 + 1000 * 999)
+    ids = [srv2.submit(*bodies(n), run(gi, n), 10) for n in (3000, 300, 1000)]
+    srv2.round()
+    assert [srv2.query(i).steps_done for i in ids] == [0, 10, 10]
+    with pytest.raises(gi.GIError):
+        gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=10**9, policy=7)
