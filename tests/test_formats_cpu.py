@@ -131,6 +131,7 @@ STRUCTS = {
     "gi_generation_plan": "GenerationPlan", "gi_earth_moon": "EarthMoon",
     "gi_generate_report": "GenerateReport", "gi_add_time_report": "AddTimeReport",
     "gi_disk_info": "DiskInfo", "gi_options": "Options", "gi_view": "View",
+    "gi_server_config": "ServerConfig",
 }
 
 
