@@ -97,6 +97,24 @@ def dist_setup(backend):
     return rank, local, world
 
 
+def max_over_ranks(x: float, device: str = "cpu") -> float:
+    """The largest value of x over the ranks (x itself with one process):
+    the timed region of a multi-GPU run is its slowest rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(interactions_per_step: int, steps: int, max_ms: float, world: int) -> float:
+    """Whole-job interactions/s of `world` independent replicas, each doing
+    the same work, timed by the slowest one (weak scaling)."""
+    return world * interactions_per_step * steps / (max_ms * 1e-3)
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
 
@@ -780,13 +798,10 @@ def run_ours(a):
     clk = clocks.stop()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
     total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, "cuda")
     ms = total_ms / a.steps
     inter = n * (n - 1)
-    value = world * inter * a.steps / (total_ms * 1e-3)
+    value = replica_value(inter, a.steps, total_ms, world)
     dp, dv = bufs[(nw + a.steps) % 2]
     state_ok = bool(torch.isfinite(dp).all().item() and torch.isfinite(dv).all().item())
 
