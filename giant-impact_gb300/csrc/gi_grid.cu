@@ -338,19 +338,22 @@ __device__ __forceinline__ unsigned long long make_item(unsigned int b, unsigned
     return ((unsigned long long)b << 37) | ((unsigned long long)c << 5) | (unsigned long long)q;
 }
 
-// Pass 2, one thread per bucket: a dense bucket of one cell becomes tiled
-// and gets an item per (chunk, distinct non-empty neighbour bucket).
+// Pass 2, one thread per bucket: a dense bucket of one cell becomes tiled,
+// is listed in tiled[0 .. *ntiled) and gets an item per (chunk, distinct
+// non-empty neighbour bucket).
 __global__ void __launch_bounds__(256)
 dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
                    const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
                    unsigned int m, unsigned int mask, unsigned int dmin, unsigned int *state,
-                   unsigned long long *__restrict__ items, unsigned int *__restrict__ nitems)
+                   unsigned long long *__restrict__ items, unsigned int *__restrict__ nitems,
+                   unsigned int *__restrict__ tiled, unsigned int *__restrict__ ntiled)
 {
     dmin = max(dmin, kDenseFloor);
     for (unsigned int b = blockIdx.x * blockDim.x + threadIdx.x; b < m; b += gridDim.x * blockDim.x) {
         const unsigned int cnt = bucket_size(cursor, b);
         if (cnt < dmin || (state[b] & kMixed)) continue;
         state[b] = kTiled;
+        tiled[atomicAdd(ntiled, 1u)] = b;
         const int j0 = sorted[b ? cursor[b - 1] : 0u];
         const int r = run_of_body(tab, j0);
         const float4 p = pos[j0];
@@ -372,11 +375,105 @@ dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ Launc
     }
 }
 
+// Sub-cell of a body inside its unit cell: 4 x 4 x 4 sub-cells of D/4,
+// numbered in Morton order.
+__device__ __forceinline__ unsigned int subcell_of(float4 p)
+{
+    const auto q = [](float x) {
+        const int s = (int)((x - floorf(x)) * 4.0f);  // NaN -> 0
+        return (unsigned int)min(max(s, 0), 3);
+    };
+    const unsigned int sx = q(p.x), sy = q(p.y), sz = q(p.z);
+    return (sx & 1u) | (sy & 1u) << 1 | (sz & 1u) << 2 | (sx >> 1) << 3 | (sy >> 1) << 4 |
+           (sz >> 1) << 5;
+}
+
+// Buckets of up to kSortCap bodies are sorted in shared memory.
+constexpr unsigned int kSortCap = 8192;
+
+// Pass 3, one CTA per tiled bucket: reorder the bucket's slots by sub-cell
+// (counting sort), so that the 32 bodies of a warp, and the 32 of a
+// staged block, sit close together.  Only the order within the bucket
+// changes; the contact sums are exact integer sums, so the forces do not
+// depend on it.  A bucket above kSortCap keeps its order.
+__global__ void __launch_bounds__(256)
+dense_sort_kernel(const float4 *__restrict__ pos, const unsigned int *__restrict__ cursor,
+                  int *__restrict__ sorted, const unsigned int *__restrict__ tiled,
+                  const unsigned int *__restrict__ ntiled)
+{
+    __shared__ int sidx[kSortCap];
+    __shared__ unsigned char skey[kSortCap];
+    __shared__ unsigned int cnt[64];
+    const unsigned int total = *ntiled;
+    for (unsigned int w = blockIdx.x; w < total; w += gridDim.x) {
+        const unsigned int b = tiled[w];
+        const unsigned int beg = b ? cursor[b - 1] : 0u, n = cursor[b] - beg;
+        if (n > kSortCap) continue;  // the same for every thread of the CTA
+        __syncthreads();  // the previous bucket is written out
+        if (threadIdx.x < 64) cnt[threadIdx.x] = 0u;
+        __syncthreads();
+        for (unsigned int u = threadIdx.x; u < n; u += blockDim.x) {
+            const int j = sorted[beg + u];
+            const unsigned int k = subcell_of(pos[j]);
+            sidx[u] = j;
+            skey[u] = (unsigned char)k;
+            atomicAdd(&cnt[k], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x < 32) {  // exclusive scan of the 64 counts, two per lane
+            const unsigned int lane = threadIdx.x;
+            const unsigned int c0 = cnt[2 * lane], c1 = cnt[2 * lane + 1];
+            unsigned int incl = c0 + c1;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)lane >= o) incl += v;
+            }
+            const unsigned int excl = incl - c0 - c1;
+            cnt[2 * lane] = excl;
+            cnt[2 * lane + 1] = excl + c0;
+        }
+        __syncthreads();
+        for (unsigned int u = threadIdx.x; u < n; u += blockDim.x)
+            sorted[beg + atomicAdd(&cnt[skey[u]], 1u)] = sidx[u];
+    }
+}
+
+// Bounding box of the non-empty lanes of a warp (lo = +inf, hi = -inf for
+// an empty lane), returned to every lane.  fminf / fmaxf drop NaN.
+__device__ __forceinline__ void warp_box(float3 &lo, float3 &hi)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
+        lo.y = fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o));
+        lo.z = fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o));
+        hi.x = fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o));
+        hi.y = fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o));
+        hi.z = fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o));
+    }
+}
+
+// Lower bound, in the rounding of the pair filter, of the FP32 r2 of every
+// pair between two boxes.  Per axis, |fl(pj - pi)| >= fl(gap) because
+// rounding is monotone, and the sum of squares below has the form of the
+// filter's, so a result >= 1 proves that no pair passes r2 < 1.  A NaN term
+// (inf - inf) is dropped by fmaxf; each remaining term bounds the finite
+// pairs, and pairs with a non-finite coordinate never pass the filter.
+__device__ __forceinline__ float box_gap2(float3 ilo, float3 ihi, float3 jlo, float3 jhi)
+{
+    const float gx = fmaxf(fmaxf(__fsub_rn(jlo.x, ihi.x), __fsub_rn(ilo.x, jhi.x)), 0.0f);
+    const float gy = fmaxf(fmaxf(__fsub_rn(jlo.y, ihi.y), __fsub_rn(ilo.y, jhi.y)), 0.0f);
+    const float gz = fmaxf(fmaxf(__fsub_rn(jlo.z, ihi.z), __fsub_rn(ilo.z, jhi.z)), 0.0f);
+    return __fmaf_rn(gz, gz, __fmaf_rn(gx, gx, __fmul_rn(gy, gy)));
+}
+
 // Grid-stride over the items.  For an item the CTA holds up to 128 bodies
 // of the bucket (one per thread, all in one cell), stages the neighbour
 // bucket in shared memory 128 bodies at a time, and each thread collects
 // the tile slots within r2 < 1 of its body before evaluating the contact
-// law on those alone.
+// law on those alone.  A warp skips each staged block of 32 bodies whose
+// bounding box is provably out of reach of its own bodies' box.
 __global__ void __launch_bounds__(128)
 contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                     const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
@@ -389,10 +486,13 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
     __shared__ float4 sp[128];
     __shared__ float4 sv[128];
     __shared__ int sj[128];
+    __shared__ float3 blo[4], bhi[4];  // box of each staged block of 32
     __shared__ unsigned char hits[128 * kStride];
     __shared__ PairDev sP;
     const unsigned int total = *nitems;
     const int t = threadIdx.x;
+    const int lane = t & 31, warp = t >> 5;
+    const float kInf = __int_as_float(0x7f800000);
     unsigned char *my = hits + t * kStride;
     for (unsigned int w = blockIdx.x; w < total; w += gridDim.x) {
         const unsigned long long it = items[w];
@@ -417,25 +517,40 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
         const int i = valid ? sorted[s0 + t] : -1;
         const float4 pi = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 vi = valid ? vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float3 ilo = valid ? make_float3(pi.x, pi.y, pi.z) : make_float3(kInf, kInf, kInf);
+        float3 ihi = valid ? make_float3(pi.x, pi.y, pi.z) : make_float3(-kInf, -kInf, -kInf);
+        warp_box(ilo, ihi);
         long long ax = 0, ay = 0, az = 0;
         for (unsigned int base = nbeg; base < nend; base += 128u) {
             __syncthreads();  // the previous tile is consumed; sP is written
             const unsigned int u = base + (unsigned int)t;
+            float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
             if (u < nend) {
                 const int j = sorted[u];
+                const float4 q = pos[j];
                 sj[t] = j;
-                sp[t] = pos[j];
+                sp[t] = q;
                 sv[t] = vel[j];
+                lo = hi = make_float3(q.x, q.y, q.z);
+            }
+            warp_box(lo, hi);
+            if (lane == 0) {
+                blo[warp] = lo;
+                bhi[warp] = hi;
             }
             __syncthreads();
             if (!valid) continue;
             const int cnt = (int)min(128u, nend - base);
             int nh = 0;
-            for (int k = 0; k < cnt; ++k) {
-                const float4 pj = sp[k];
-                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-                if (r2 < 1.0f) my[nh++] = (unsigned char)k;
+            for (int s = 0; s < 4 && 32 * s < cnt; ++s) {
+                if (box_gap2(ilo, ihi, blo[s], bhi[s]) >= 1.0f) continue;  // the same for the warp
+                const int k1 = min(cnt, 32 * s + 32);
+                for (int k = 32 * s; k < k1; ++k) {
+                    const float4 pj = sp[k];
+                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+                    if (r2 < 1.0f) my[nh++] = (unsigned char)k;
+                }
             }
             for (int h = 0; h < nh; ++h) {
                 const int k = my[h];
@@ -478,13 +593,19 @@ static size_t dense_item_capacity(long long bodies)
     return 27 * ((size_t)bodies / 128 + (size_t)bodies / gi::kDenseFloor + 2);
 }
 
+// Tiled buckets: each holds at least kDenseFloor bodies.
+static size_t dense_bucket_capacity(long long bodies)
+{
+    return (size_t)bodies / gi::kDenseFloor + 1;
+}
+
 // keys + sorted: `bodies` each (indexed by global body index / slot); cursor
-// and bucket state: one word per bucket each; block sums: 8192; item count
-// (2 words) and items (2 words each).
+// and bucket state: one word per bucket each; block sums: 8192; item and
+// tiled-bucket counts (2 words); items (2 words each); tiled buckets.
 size_t gi_grid_words(long long max_end, long long bodies)
 {
     return 2 * (size_t)max_end + 2 * (size_t)gi_grid_buckets(bodies) + 8192 + 2 +
-           2 * dense_item_capacity(bodies);
+           2 * dense_item_capacity(bodies) + dense_bucket_capacity(bodies);
 }
 
 cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, cudaStream_t s)
@@ -510,7 +631,9 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     unsigned int *state = cursor + m;
     unsigned int *sums = state + m;
     unsigned int *nitems = sums + 8192;
+    unsigned int *ntiled = nitems + 1;
     unsigned long long *items = reinterpret_cast<unsigned long long *>(nitems + 2);  // 8-byte aligned
+    unsigned int *tiled = reinterpret_cast<unsigned int *>(items + dense_item_capacity(bodies));
     int maxn = 0;
     for (int r = 0; r < tab.nruns; ++r) maxn = std::max(maxn, tab.runs[r].n);
     if (maxn == 0) return cudaSuccess;
@@ -518,7 +641,7 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(state, 0, (size_t)m * sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(nitems, 0, sizeof(unsigned int), s);
+    e = cudaMemsetAsync(nitems, 0, 2 * sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
     const dim3 gk(std::min(4 * nsm, (maxn + 255) / 256), tab.nruns);
     gi::grid_keys<<<gk, 256, 0, s>>>(pos, tab, m - 1, keys, cursor);
@@ -530,7 +653,8 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     const unsigned int dmin = (unsigned int)tab.dense_min;
     gi::dense_check_kernel<<<gk, 256, 0, s>>>(pos, tab, keys, cursor, sorted, dmin, state, delta);
     gi::dense_items_kernel<<<std::min((int)((m + 255) / 256), 4 * nsm), 256, 0, s>>>(
-        pos, tab, cursor, sorted, m, m - 1, dmin, state, items, nitems);
+        pos, tab, cursor, sorted, m, m - 1, dmin, state, items, nitems, tiled, ntiled);
+    gi::dense_sort_kernel<<<2 * nsm, 256, 0, s>>>(pos, cursor, sorted, tiled, ntiled);
     const dim3 gc((maxn + 7) / 8, tab.nruns);
     gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, cursor, sorted, keys, state, m - 1, delta, tab);
     gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(pos, vel, cursor, sorted, m - 1, delta, tab,

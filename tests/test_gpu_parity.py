@@ -460,3 +460,52 @@ def test_dense_contact_path_matches_sparse_path(gi, orc, torch_cuda):
     err = rel_l2(ft[idx, :3], f64)
     print(f"dense remnant: rel L2 vs FP64 {err:.3e}")
     assert err < FORCE_TOL
+
+
+@pytest.mark.gpu
+def test_dense_contact_path_crowded_cells(gi, orc, torch_cuda):
+    """Cells of hundreds of bodies (several 128-body chunks and neighbour
+    tiles, reordered by sub-cell), one cell of 9,000 bodies (above the
+    in-bucket sort's capacity, so left in scatter order) and two runs laid
+    over the same space (their buckets must stay apart): the tiled path
+    equals the warp path bit for bit, repeats bit for bit, and stays within
+    the force tolerance of the FP64 oracle."""
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    rng = np.random.default_rng(29)
+
+    def ball(n, radius, centre):
+        d = rng.normal(size=(n, 3))
+        d = d / np.linalg.norm(d, axis=1, keepdims=True) * (rng.uniform(0, 1, size=(n, 1)) ** (1 / 3))
+        return d * radius + np.asarray(centre)
+
+    run_a = np.concatenate([ball(10000, 1.8, (0.0, 0.0, 0.0)),
+                            rng.uniform(0.05, 0.95, size=(9000, 3)) + np.array([30.0, 0.0, 0.0])])
+    run_b = ball(6000, 1.6, (0.3, 0.2, 0.1))
+    pos = np.zeros((len(run_a) + len(run_b), 4), np.float32)
+    pos[:len(run_a), :3] = run_a
+    pos[len(run_a):, :3] = run_b
+    vel = np.zeros_like(pos)
+    vel[:, :3] = rng.normal(scale=2.0, size=(len(pos), 3)).astype(np.float32)
+    vel[:, 3] = 0.4
+    nfe_a, nfe_b = 3000, 1000
+    runs = [wl.run_desc(gi, 0, len(run_a), nfe_a), wl.run_desc(gi, len(run_a), len(run_b), nfe_b)]
+    tiled = gi.Context(0, dense_min=64)
+    warp = gi.Context(0, dense_min=1 << 30)
+    ft = gpu_forces(gi, torch, tiled, pos, vel, runs, p)
+    fw = gpu_forces(gi, torch, warp, pos, vel, runs, p)
+    ft2 = gpu_forces(gi, torch, tiled, pos, vel, runs, p)
+    tiled.close()
+    warp.close()
+    assert np.isfinite(ft[:, :3]).all()
+    assert np.array_equal(ft[:, :3], fw[:, :3])
+    assert np.array_equal(ft[:, :3], ft2[:, :3])
+    na = len(run_a)
+    for off, n, nfe, step in ((0, na, nfe_a, 37), (na, len(run_b), nfe_b, 29)):
+        idx = np.arange(off, off + n, step).astype(np.int32)
+        sub_pos, sub_vel = pos[off:off + n], vel[off:off + n]
+        f64, _ = orc.forces_fp64(sub_pos, sub_vel, [(0, n, nfe, 0, 0, 0, 0, 0)], p, idx=idx - off)
+        err = rel_l2(ft[idx, :3], f64)
+        print(f"crowded cells, run at {off}: rel L2 vs FP64 {err:.3e}")
+        assert err < FORCE_TOL
