@@ -138,33 +138,65 @@ grid_scatter(const __grid_constant__ LaunchTable tab, const unsigned int *__rest
     }
 }
 
-// Contact correction of one pair, as a coefficient of dp in force units:
-// the reference law's contact force on i, mag dp / r, minus the clamped
-// far-field term gm_i gm_j r2c^-3/2 dp the all-pairs pass added.
-__device__ __forceinline__ float contact_coef(const PairDev &P, int sep_test, int i, int j,
-                                              int sw, float dx, float dy, float dz, float r2,
-                                              float4 vi, float4 vj)
+// Pair constants of body i against a j of one material: the class row of
+// the table and the far-field term of a contact pair.
+struct PairRow {
+    float G, K, Tband, Tmid, KRmid, KRin;
+    float far;  // -(gm_i gm_j) s_far, the clamped far-field coefficient at r2 < 1
+};
+
+__device__ __forceinline__ PairRow pair_row(const PairDev &P, bool ife, bool jfe)
 {
-    const int test = (i < sw) + (j < sw);
-    const float G = P.G[test];
-    float K = P.K[test];
-    if (!(r2 >= P.Tband[test])) {
+    const int test = (int)ife + (int)jfe;
+    PairRow w;
+    w.G = P.G[test];
+    w.K = P.K[test];
+    w.Tband = P.Tband[test];
+    w.Tmid = P.Tmid[test];
+    w.KRmid = P.KRmid[test];
+    w.KRin = P.KRin[test];
+    // every contact pair has r2 < 1, where the all-pairs pass clamps r2 to 1
+    const float ri = rsqrt_mufu(1.0f);
+    const float s_far = (ri * ri) * ri;
+    const float gmi = ife ? P.gm_fe : P.gm_si;
+    const float gmj = jfe ? P.gm_fe : P.gm_si;
+    w.far = -(gmi * gmj) * s_far;
+    return w;
+}
+
+__device__ __forceinline__ PairRow select_row(bool jfe, const PairRow &fe, const PairRow &si)
+{
+    PairRow w;
+    w.G = jfe ? fe.G : si.G;
+    w.K = jfe ? fe.K : si.K;
+    w.Tband = jfe ? fe.Tband : si.Tband;
+    w.Tmid = jfe ? fe.Tmid : si.Tmid;
+    w.KRmid = jfe ? fe.KRmid : si.KRmid;
+    w.KRin = jfe ? fe.KRin : si.KRin;
+    w.far = jfe ? fe.far : si.far;
+    return w;
+}
+
+// Contact correction of one pair with r2 < 1, as a coefficient of dp in
+// force units: the reference law's contact force on i, mag dp / r, minus
+// the clamped far-field term gm_i gm_j dp the all-pairs pass added.
+__device__ __forceinline__ float contact_coef(const PairRow &w, int sep_test, float dx, float dy,
+                                              float dz, float r2, float4 vi, float4 vj)
+{
+    float K = w.K;
+    if (!(r2 >= w.Tband)) {
         const float dvx = __fsub_rn(vj.x, vi.x), dvy = __fsub_rn(vj.y, vi.y),
                     dvz = __fsub_rn(vj.z, vi.z);
         const float dpdv = __fmaf_rn(dz, dvz, __fmaf_rn(dx, dvx, __fmul_rn(dy, dvy)));
         // Reference: int inout = dp.dv; KR when inout > 0, i.e. dp.dv >= 1.
         const bool sep = (sep_test == GI_SEP_SIGN) ? (dpdv > 0.0f) : (dpdv >= 1.0f);
-        if (sep) K = (r2 >= P.Tmid[test]) ? P.KRmid[test] : P.KRin[test];
+        if (sep) K = (r2 >= w.Tmid) ? w.KRmid : w.KRin;
     }
-    const float mag = contact_mag(G, K, r2);
+    const float mag = contact_mag(w.G, K, r2);
     // 1 / r: MUFU rsqrt and one Newton-Raphson step (about 1 ulp)
     float invr = rsqrt_mufu(r2);
     invr = invr * __fmaf_rn(-0.5f * r2 * invr, invr, 1.5f);
-    const float ri = rsqrt_mufu(fmaxf(r2, 1.0f));
-    const float s_far = (ri * ri) * ri;
-    const float gmi = (i < sw) ? P.gm_fe : P.gm_si;
-    const float gmj = (j < sw) ? P.gm_fe : P.gm_si;
-    return __fmaf_rn(mag, invr, -(gmi * gmj) * s_far);
+    return __fmaf_rn(mag, invr, w.far);
 }
 
 // Buckets of at least tab.dense_min bodies (256 unless set) whose bodies
@@ -173,18 +205,6 @@ __device__ __forceinline__ float contact_coef(const PairDev &P, int sep_test, in
 // path), 2 = tiled.
 constexpr unsigned int kDenseFloor = 32;
 constexpr unsigned int kMixed = 1u, kTiled = 2u;
-
-// Copy of a pair table into shared memory by the first threads of the CTA,
-// so that lanes indexing it by pair class read banks rather than serialise
-// on the constant cache.
-__device__ __forceinline__ void stage_pairs(PairDev &dst, const PairDev &src)
-{
-    static_assert(sizeof(PairDev) % 4 == 0, "PairDev is copied word by word");
-    constexpr int kWords = (int)(sizeof(PairDev) / 4);
-    if ((int)threadIdx.x < kWords)
-        reinterpret_cast<unsigned int *>(&dst)[threadIdx.x] =
-            reinterpret_cast<const unsigned int *>(&src)[threadIdx.x];
-}
 
 // Contact correction of body i (run r) by one warp.  Lanes 0..26 look up
 // the 27 neighbour buckets at once (one memory round trip; a bucket that
@@ -224,6 +244,7 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
     const unsigned int excl = incl - cnt;
 
     const float inv_unit = (float)(1.0 / P.fx_unit);
+    const PairRow row_fe = pair_row(P, i < sw, true), row_si = pair_row(P, i < sw, false);
     float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
     bool have_vi = false;
     long long ax = 0, ay = 0, az = 0;
@@ -247,7 +268,9 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
         if (!(r2 < 1.0f)) continue;
         if (!have_vi) { vi = __ldg(&vel[i]); have_vi = true; }
         const float4 vj = __ldg(&vel[j]);
-        const float c = contact_coef(P, sep_test, i, j, sw, dx, dy, dz, r2, vi, vj) * inv_unit;
+        const float c =
+            contact_coef(select_row(j < sw, row_fe, row_si), sep_test, dx, dy, dz, r2, vi, vj) *
+            inv_unit;
         ax += __float2ll_rn(c * dx);
         ay += __float2ll_rn(c * dy);
         az += __float2ll_rn(c * dz);
@@ -280,17 +303,14 @@ contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                unsigned int mask, long long *__restrict__ delta,
                const __grid_constant__ LaunchTable tab)
 {
-    __shared__ PairDev sP;
     const RunDev &R = tab.runs[blockIdx.y];
-    stage_pairs(sP, tab.params[R.param]);
-    __syncthreads();
     const int lane = threadIdx.x & 31;
     const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (k >= R.n) return;  // whole warp leaves together
     const int i = R.offset + k;
     if (state[__ldg(&keys[i])] & kTiled) return;
-    contact_body_warp(pos, vel, cursor, sorted, mask, delta, R, sP, tab.sep_test, blockIdx.y, i,
-                      lane);
+    contact_body_warp(pos, vel, cursor, sorted, mask, delta, R, tab.params[R.param], tab.sep_test,
+                      blockIdx.y, i, lane);
 }
 
 // Pass 1, one thread per body of the run blockIdx.y: for bodies of dense
@@ -483,12 +503,10 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
                     const unsigned int *__restrict__ nitems)
 {
     constexpr int kStride = 132;  // bytes per hit list row: rows start in distinct banks
-    __shared__ float4 sp[128];
+    __shared__ float4 sp[128];  // x, y, z, body index (bits); NaN xyz outside the run
     __shared__ float4 sv[128];
-    __shared__ int sj[128];
     __shared__ float3 blo[4], bhi[4];  // box of each staged block of 32
     __shared__ unsigned char hits[128 * kStride];
-    __shared__ PairDev sP;
     const unsigned int total = *nitems;
     const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
@@ -505,8 +523,6 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
         const int j0 = sorted[s0];  // every item's chunk holds at least one body
         const int run = run_of_body(tab, j0);
         const RunDev &R = tab.runs[run];
-        __syncthreads();  // every thread is done with the previous item's table
-        stage_pairs(sP, tab.params[R.param]);
         const int rbeg = R.offset, rend = R.offset + R.n, sw = R.offset + R.nfe;
         const float inv_unit = (float)(1.0 / tab.params[R.param].fx_unit);
         const float4 p0 = pos[j0];
@@ -517,21 +533,27 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
         const int i = valid ? sorted[s0 + t] : -1;
         const float4 pi = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 vi = valid ? vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const PairRow row_fe = pair_row(tab.params[R.param], i < sw, true);
+        const PairRow row_si = pair_row(tab.params[R.param], i < sw, false);
         float3 ilo = valid ? make_float3(pi.x, pi.y, pi.z) : make_float3(kInf, kInf, kInf);
         float3 ihi = valid ? make_float3(pi.x, pi.y, pi.z) : make_float3(-kInf, -kInf, -kInf);
         warp_box(ilo, ihi);
         long long ax = 0, ay = 0, az = 0;
         for (unsigned int base = nbeg; base < nend; base += 128u) {
-            __syncthreads();  // the previous tile is consumed; sP is written
+            __syncthreads();  // the previous tile is consumed
             const unsigned int u = base + (unsigned int)t;
             float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
             if (u < nend) {
                 const int j = sorted[u];
-                const float4 q = pos[j];
-                sj[t] = j;
-                sp[t] = q;
-                sv[t] = vel[j];
-                lo = hi = make_float3(q.x, q.y, q.z);
+                if (j >= rbeg && j < rend) {
+                    const float4 q = pos[j];
+                    sp[t] = make_float4(q.x, q.y, q.z, __int_as_float(j));
+                    sv[t] = vel[j];
+                    lo = hi = make_float3(q.x, q.y, q.z);
+                } else {  // another run's body, in a bucket shared by hashing: never a hit
+                    const float nan = __int_as_float(0x7fffffff);
+                    sp[t] = make_float4(nan, nan, nan, __int_as_float(j));
+                }
             }
             warp_box(lo, hi);
             if (lane == 0) {
@@ -554,13 +576,14 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
             }
             for (int h = 0; h < nh; ++h) {
                 const int k = my[h];
-                const int j = sj[k];
-                if (j == i || j < rbeg || j >= rend) continue;
                 const float4 pj = sp[k];
+                const int j = __float_as_int(pj.w);
+                if (j == i) continue;
                 const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
                 const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-                const float c =
-                    contact_coef(sP, tab.sep_test, i, j, sw, dx, dy, dz, r2, vi, sv[k]) * inv_unit;
+                const float c = contact_coef(select_row(j < sw, row_fe, row_si), tab.sep_test, dx,
+                                             dy, dz, r2, vi, sv[k]) *
+                                inv_unit;
                 ax += __float2ll_rn(c * dx);
                 ay += __float2ll_rn(c * dy);
                 az += __float2ll_rn(c * dz);
