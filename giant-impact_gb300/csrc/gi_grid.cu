@@ -199,6 +199,77 @@ __device__ __forceinline__ float contact_coef(const PairRow &w, int sep_test, fl
     return __fmaf_rn(mag, invr, w.far);
 }
 
+// Fixed-point sums without the FP64 unit.  Each pair term x (FP32, in
+// units of the fixed point) is rounded to the nearest integer, ties to
+// even, exactly as cvt.rni.s64.f32 would; that instruction issues on the
+// FP64 unit, the slowest unit of this GPU, so the terms are split on the
+// FP32 pipe instead.  For |x| < 2^45:
+//   s = fl(x + 1.5 2^46) is x rounded to a multiple of 2^23 (ulp 2^23) plus
+//       1.5 2^46, and stays in [2^46, 2^47], so its bit pattern minus that
+//       of 1.5 2^46 is hi = (s - 1.5 2^46) / 2^23;
+//   lo = x - hi 2^23 is exact (|lo| <= 2^22), and fl(lo + 1.5 2^23) rounds
+//       it to an integer (ulp 1, ties to even), read back the same way.
+// round(x) = hi 2^23 + round(lo) because 2^23 is even.  Bit patterns are
+// summed mod 2^32 and folded into 64 bits at most every kFixFold terms,
+// before the 32-bit sums of hi and lo (each |.| <= 2^22 a term) can wrap.
+constexpr float kFixM = 0x1.8p46f;  // 1.5 * 2^46
+constexpr float kFixC = 0x1.8p23f;  // 1.5 * 2^23
+constexpr float kFixMax = 0x1p45f;  // largest |term| the split takes
+constexpr unsigned int kFixFold = 256;
+
+struct FixSum3 {
+    long long x, y, z;           // folded sums
+    unsigned int hx, hy, hz;     // pending bit-pattern sums of s
+    unsigned int lx, ly, lz;     // pending bit-pattern sums of fl(lo + 1.5 2^23)
+    unsigned int n;              // pending terms
+};
+
+__device__ __forceinline__ void fix_zero(FixSum3 &a)
+{
+    a.x = a.y = a.z = 0;
+    a.hx = a.hy = a.hz = a.lx = a.ly = a.lz = a.n = 0u;
+}
+
+__device__ __forceinline__ void fix_split(float x, unsigned int &h, unsigned int &l)
+{
+    const float s = __fadd_rn(x, kFixM);
+    const float lo = __fsub_rn(x, __fsub_rn(s, kFixM));
+    h += __float_as_uint(s);
+    l += __float_as_uint(__fadd_rn(lo, kFixC));
+}
+
+__device__ __forceinline__ long long fix_value(unsigned int h, unsigned int l, unsigned int n)
+{
+    const int hi = (int)(h - n * __float_as_uint(kFixM));
+    const int lo = (int)(l - n * __float_as_uint(kFixC));
+    return (long long)hi * (1ll << 23) + lo;
+}
+
+__device__ __forceinline__ void fix_fold(FixSum3 &a)
+{
+    a.x += fix_value(a.hx, a.lx, a.n);
+    a.y += fix_value(a.hy, a.ly, a.n);
+    a.z += fix_value(a.hz, a.lz, a.n);
+    a.hx = a.hy = a.hz = a.lx = a.ly = a.lz = a.n = 0u;
+}
+
+// Adds round(c dx), round(c dy), round(c dz).  Terms out of the split's
+// range (a pair at r ~ 0, or NaN) take the hardware conversion.
+__device__ __forceinline__ void fix_add3(FixSum3 &a, float c, float dx, float dy, float dz)
+{
+    const float tx = __fmul_rn(c, dx), ty = __fmul_rn(c, dy), tz = __fmul_rn(c, dz);
+    if (fabsf(tx) < kFixMax && fabsf(ty) < kFixMax && fabsf(tz) < kFixMax) {
+        fix_split(tx, a.hx, a.lx);
+        fix_split(ty, a.hy, a.ly);
+        fix_split(tz, a.hz, a.lz);
+        if (++a.n == kFixFold) fix_fold(a);
+    } else {
+        a.x += __float2ll_rn(tx);
+        a.y += __float2ll_rn(ty);
+        a.z += __float2ll_rn(tz);
+    }
+}
+
 // Buckets of at least tab.dense_min bodies (256 unless set) whose bodies
 // share one cell take the tiled path; at least kDenseFloor, which bounds
 // the item count.  Bucket state bits: 1 = mixed cells (stays on the warp
@@ -247,7 +318,8 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
     const PairRow row_fe = pair_row(P, i < sw, true), row_si = pair_row(P, i < sw, false);
     float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
     bool have_vi = false;
-    long long ax = 0, ay = 0, az = 0;
+    FixSum3 acc;
+    fix_zero(acc);
     for (unsigned int base = 0; base < total; base += 32) {
         const unsigned int t = base + lane;
         // the lane whose range [excl, incl) holds t: last lane with excl <= t
@@ -271,10 +343,10 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
         const float c =
             contact_coef(select_row(j < sw, row_fe, row_si), sep_test, dx, dy, dz, r2, vi, vj) *
             inv_unit;
-        ax += __float2ll_rn(c * dx);
-        ay += __float2ll_rn(c * dy);
-        az += __float2ll_rn(c * dz);
+        fix_add3(acc, c, dx, dy, dz);
     }
+    fix_fold(acc);
+    long long ax = acc.x, ay = acc.y, az = acc.z;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         ax += __shfl_down_sync(0xffffffffu, ax, off);
@@ -538,7 +610,8 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
         float3 ilo = valid ? make_float3(pi.x, pi.y, pi.z) : make_float3(kInf, kInf, kInf);
         float3 ihi = valid ? make_float3(pi.x, pi.y, pi.z) : make_float3(-kInf, -kInf, -kInf);
         warp_box(ilo, ihi);
-        long long ax = 0, ay = 0, az = 0;
+        FixSum3 acc;
+        fix_zero(acc);
         for (unsigned int base = nbeg; base < nend; base += 128u) {
             __syncthreads();  // the previous tile is consumed
             const unsigned int u = base + (unsigned int)t;
@@ -584,11 +657,11 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
                 const float c = contact_coef(select_row(j < sw, row_fe, row_si), tab.sep_test, dx,
                                              dy, dz, r2, vi, sv[k]) *
                                 inv_unit;
-                ax += __float2ll_rn(c * dx);
-                ay += __float2ll_rn(c * dy);
-                az += __float2ll_rn(c * dz);
+                fix_add3(acc, c, dx, dy, dz);
             }
         }
+        fix_fold(acc);
+        const long long ax = acc.x, ay = acc.y, az = acc.z;
         if (valid && (ax | ay | az)) {
             unsigned long long *d = reinterpret_cast<unsigned long long *>(delta + 3 * (size_t)i);
             atomicAdd(d + 0, (unsigned long long)ax);
