@@ -561,12 +561,16 @@ __device__ __forceinline__ float box_gap2(float3 ilo, float3 ihi, float3 jlo, fl
 }
 
 // Grid-stride over the items.  For an item the CTA holds up to 128 bodies
-// of the bucket (one per thread, all in one cell), stages the neighbour
-// bucket in shared memory 128 bodies at a time, and each thread collects
-// the tile slots within r2 < 1 of its body before evaluating the contact
-// law on those alone.  A warp skips each staged block of 32 bodies whose
-// bounding box is provably out of reach of its own bodies' box.
-__global__ void __launch_bounds__(128)
+// of the bucket (one per thread, all in one cell) and stages the neighbour
+// bucket in shared memory kTileJ bodies at a time.  Each thread then works
+// through the staged bodies 128 at a time: it collects the slots within
+// r2 < 1 of its body, then evaluates the contact law on those alone.  A
+// warp skips each staged block of 32 bodies whose bounding box is provably
+// out of reach of its own bodies' box.  One barrier pair per kTileJ staged
+// bodies lets the warps' uneven hit counts even out between barriers.
+constexpr int kTileJ = 256;
+
+__global__ void __launch_bounds__(128, 8)
 contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                     const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
                     unsigned int mask, long long *__restrict__ delta,
@@ -575,9 +579,10 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
                     const unsigned int *__restrict__ nitems)
 {
     constexpr int kStride = 132;  // bytes per hit list row: rows start in distinct banks
-    __shared__ float4 sp[128];  // x, y, z, body index (bits); NaN xyz outside the run
-    __shared__ float4 sv[128];
-    __shared__ float3 blo[4], bhi[4];  // box of each staged block of 32
+    constexpr int kBlocks = kTileJ / 32;
+    __shared__ float4 sp[kTileJ];  // x, y, z, body index (bits); NaN xyz outside the run
+    __shared__ float4 sv[kTileJ];
+    __shared__ float3 blo[kBlocks], bhi[kBlocks];  // box of each staged block of 32
     __shared__ unsigned char hits[128 * kStride];
     const unsigned int total = *nitems;
     const int t = threadIdx.x;
@@ -612,52 +617,58 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
         warp_box(ilo, ihi);
         FixSum3 acc;
         fix_zero(acc);
-        for (unsigned int base = nbeg; base < nend; base += 128u) {
+        for (unsigned int base = nbeg; base < nend; base += (unsigned int)kTileJ) {
             __syncthreads();  // the previous tile is consumed
-            const unsigned int u = base + (unsigned int)t;
-            float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
-            if (u < nend) {
-                const int j = sorted[u];
-                if (j >= rbeg && j < rend) {
-                    const float4 q = pos[j];
-                    sp[t] = make_float4(q.x, q.y, q.z, __int_as_float(j));
-                    sv[t] = vel[j];
-                    lo = hi = make_float3(q.x, q.y, q.z);
-                } else {  // another run's body, in a bucket shared by hashing: never a hit
-                    const float nan = __int_as_float(0x7fffffff);
-                    sp[t] = make_float4(nan, nan, nan, __int_as_float(j));
+#pragma unroll
+            for (int r = 0; r < kTileJ / 128; ++r) {
+                const int slot = 128 * r + t;
+                const unsigned int u = base + (unsigned int)slot;
+                float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
+                if (u < nend) {
+                    const int j = sorted[u];
+                    if (j >= rbeg && j < rend) {
+                        const float4 q = pos[j];
+                        sp[slot] = make_float4(q.x, q.y, q.z, __int_as_float(j));
+                        sv[slot] = vel[j];
+                        lo = hi = make_float3(q.x, q.y, q.z);
+                    } else {  // another run's body, in a bucket shared by hashing: never a hit
+                        const float nan = __int_as_float(0x7fffffff);
+                        sp[slot] = make_float4(nan, nan, nan, __int_as_float(j));
+                    }
                 }
-            }
-            warp_box(lo, hi);
-            if (lane == 0) {
-                blo[warp] = lo;
-                bhi[warp] = hi;
+                warp_box(lo, hi);
+                if (lane == 0) {
+                    blo[4 * r + warp] = lo;
+                    bhi[4 * r + warp] = hi;
+                }
             }
             __syncthreads();
             if (!valid) continue;
-            const int cnt = (int)min(128u, nend - base);
-            int nh = 0;
-            for (int s = 0; s < 4 && 32 * s < cnt; ++s) {
-                if (box_gap2(ilo, ihi, blo[s], bhi[s]) >= 1.0f) continue;  // the same for the warp
-                const int k1 = min(cnt, 32 * s + 32);
-                for (int k = 32 * s; k < k1; ++k) {
+            const int cnt = (int)min((unsigned int)kTileJ, nend - base);
+            for (int h0 = 0; h0 < cnt; h0 += 128) {
+                int nh = 0;
+                for (int s = h0 / 32; s < h0 / 32 + 4 && 32 * s < cnt; ++s) {
+                    if (box_gap2(ilo, ihi, blo[s], bhi[s]) >= 1.0f) continue;  // warp-uniform
+                    const int k1 = min(cnt, 32 * s + 32);
+                    for (int k = 32 * s; k < k1; ++k) {
+                        const float4 pj = sp[k];
+                        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+                        if (r2 < 1.0f) my[nh++] = (unsigned char)(k - h0);
+                    }
+                }
+                for (int hh = 0; hh < nh; ++hh) {
+                    const int k = h0 + my[hh];
                     const float4 pj = sp[k];
+                    const int j = __float_as_int(pj.w);
+                    if (j == i) continue;
                     const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
                     const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-                    if (r2 < 1.0f) my[nh++] = (unsigned char)k;
+                    const float c = contact_coef(select_row(j < sw, row_fe, row_si), tab.sep_test,
+                                                 dx, dy, dz, r2, vi, sv[k]) *
+                                    inv_unit;
+                    fix_add3(acc, c, dx, dy, dz);
                 }
-            }
-            for (int h = 0; h < nh; ++h) {
-                const int k = my[h];
-                const float4 pj = sp[k];
-                const int j = __float_as_int(pj.w);
-                if (j == i) continue;
-                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-                const float c = contact_coef(select_row(j < sw, row_fe, row_si), tab.sep_test, dx,
-                                             dy, dz, r2, vi, sv[k]) *
-                                inv_unit;
-                fix_add3(acc, c, dx, dy, dz);
             }
         }
         fix_fold(acc);
