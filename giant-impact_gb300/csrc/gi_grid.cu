@@ -270,6 +270,62 @@ __device__ __forceinline__ void fix_add3(FixSum3 &a, float c, float dx, float dy
     }
 }
 
+// Pair form of fix_add3 for an unordered pair evaluated once: adds
+// round(c d) to body i's sums and -round(c d), exactly the term body j's own
+// evaluation would give (dp and dv change sign exactly, c is symmetric, and
+// rounding to nearest even is odd-symmetric), to the shared sums js[.][k]
+// of j's staged slot: true values mod 2^32, hi in js[0..2], lo in js[3..5].
+// A term out of the split's range goes to j's global sums directly.
+__device__ __forceinline__ void fix_add3_pair(FixSum3 &a, unsigned int (*js)[128], int k,
+                                              long long *dj, float c, float dx, float dy, float dz)
+{
+    const float tx = __fmul_rn(c, dx), ty = __fmul_rn(c, dy), tz = __fmul_rn(c, dz);
+    if (fabsf(tx) < kFixMax && fabsf(ty) < kFixMax && fabsf(tz) < kFixMax) {
+        const float t3[3] = {tx, ty, tz};
+        unsigned int *h3[3] = {&a.hx, &a.hy, &a.hz};
+        unsigned int *l3[3] = {&a.lx, &a.ly, &a.lz};
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float sd = __fadd_rn(t3[d], kFixM);
+            const float ld = __fadd_rn(__fsub_rn(t3[d], __fsub_rn(sd, kFixM)), kFixC);
+            *h3[d] += __float_as_uint(sd);
+            *l3[d] += __float_as_uint(ld);
+            atomicAdd(&js[d][k], __float_as_uint(kFixM) - __float_as_uint(sd));
+            atomicAdd(&js[3 + d][k], __float_as_uint(kFixC) - __float_as_uint(ld));
+        }
+        if (++a.n == kFixFold) fix_fold(a);
+    } else {
+        const long long vx = __float2ll_rn(tx), vy = __float2ll_rn(ty), vz = __float2ll_rn(tz);
+        a.x += vx;
+        a.y += vy;
+        a.z += vz;
+        unsigned long long *d = reinterpret_cast<unsigned long long *>(dj);
+        atomicAdd(d + 0, 0ull - (unsigned long long)vx);
+        atomicAdd(d + 1, 0ull - (unsigned long long)vy);
+        atomicAdd(d + 2, 0ull - (unsigned long long)vz);
+    }
+}
+
+// Adds the shared j-side sums of slot t to body j's correction and clears them.
+__device__ __forceinline__ void flush_slot(unsigned int (*js)[128], int t, int j, long long *delta)
+{
+    long long v[3];
+    bool any = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        v[d] = (long long)(int)js[d][t] * (1ll << 23) + (int)js[3 + d][t];
+        any |= v[d] != 0;
+        js[d][t] = 0u;
+        js[3 + d][t] = 0u;
+    }
+    if (any) {
+        unsigned long long *p = reinterpret_cast<unsigned long long *>(delta + 3 * (size_t)j);
+        atomicAdd(p + 0, (unsigned long long)v[0]);
+        atomicAdd(p + 1, (unsigned long long)v[1]);
+        atomicAdd(p + 2, (unsigned long long)v[2]);
+    }
+}
+
 // Buckets of at least tab.dense_min bodies (256 unless set) whose bodies
 // share one cell take the tiled path; at least kDenseFloor, which bounds
 // the item count.  Bucket state bits: 1 = mixed cells (stays on the warp
@@ -430,40 +486,58 @@ __device__ __forceinline__ unsigned long long make_item(unsigned int b, unsigned
     return ((unsigned long long)b << 37) | ((unsigned long long)c << 5) | (unsigned long long)q;
 }
 
-// Pass 2, one thread per bucket: a dense bucket of one cell becomes tiled,
-// is listed in tiled[0 .. *ntiled) and gets an item per (chunk, distinct
-// non-empty neighbour bucket).
+// Pass 2, one thread per bucket: a dense bucket of one cell becomes tiled
+// and is listed in tiled[0 .. *ntiled).
 __global__ void __launch_bounds__(256)
-dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
-                   const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
-                   unsigned int m, unsigned int mask, unsigned int dmin, unsigned int *state,
-                   unsigned long long *__restrict__ items, unsigned int *__restrict__ nitems,
-                   unsigned int *__restrict__ tiled, unsigned int *__restrict__ ntiled)
+dense_mark_kernel(const unsigned int *__restrict__ cursor, unsigned int m, unsigned int dmin,
+                  unsigned int *state, unsigned int *__restrict__ tiled,
+                  unsigned int *__restrict__ ntiled)
 {
     dmin = max(dmin, kDenseFloor);
     for (unsigned int b = blockIdx.x * blockDim.x + threadIdx.x; b < m; b += gridDim.x * blockDim.x) {
-        const unsigned int cnt = bucket_size(cursor, b);
-        if (cnt < dmin || (state[b] & kMixed)) continue;
+        if (bucket_size(cursor, b) < dmin || (state[b] & kMixed)) continue;
         state[b] = kTiled;
         tiled[atomicAdd(ntiled, 1u)] = b;
+    }
+}
+
+// Pass 4, one thread per tiled bucket b: an item per (chunk of 128 of its
+// bodies, distinct non-empty neighbour bucket nb).  A pair of tiled
+// buckets is listed once, from the lower bucket number (nb >= b): its
+// item evaluates each contact pair once for both bodies.  A bucket that is
+// not tiled gets its own sums from contact_kernel, so its item adds to b's
+// bodies only.
+__global__ void __launch_bounds__(256)
+dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
+                   const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
+                   unsigned int mask, const unsigned int *__restrict__ state,
+                   const unsigned int *__restrict__ tiled, const unsigned int *__restrict__ ntiled,
+                   unsigned long long *__restrict__ items, unsigned int *__restrict__ nitems)
+{
+    const unsigned int total = *ntiled;
+    for (unsigned int w = blockIdx.x * blockDim.x + threadIdx.x; w < total;
+         w += gridDim.x * blockDim.x) {
+        const unsigned int b = tiled[w];
+        const unsigned int cnt = bucket_size(cursor, b);
         const int j0 = sorted[b ? cursor[b - 1] : 0u];
         const int r = run_of_body(tab, j0);
         const float4 p = pos[j0];
         const int cx = cell_of(p.x), cy = cell_of(p.y), cz = cell_of(p.z);
         unsigned int nb[27];
-        unsigned int uniq = 0;  // bit q: offset q is the first to reach its bucket
+        unsigned int keep = 0;  // bit q: offset q is the first to reach its bucket, and listed here
         for (int q = 0; q < 27; ++q) {
             nb[q] = bucket_of(r, cx + q % 3 - 1, cy + (q / 3) % 3 - 1, cz + q / 9 - 1, mask);
             bool dup = false;
             for (int u = 0; u < q; ++u) dup |= nb[u] == nb[q];
-            if (!dup && bucket_size(cursor, nb[q]) > 0) uniq |= 1u << q;
+            const bool other_side = (state[nb[q]] & kTiled) && nb[q] < b;
+            if (!dup && !other_side && bucket_size(cursor, nb[q]) > 0) keep |= 1u << q;
         }
         const unsigned int nch = (cnt + 127u) / 128u;
-        const unsigned int nq = __popc(uniq);
+        const unsigned int nq = __popc(keep);
         unsigned int at = atomicAdd(nitems, nch * nq);
         for (unsigned int c = 0; c < nch; ++c)
             for (int q = 0; q < 27; ++q)
-                if (uniq & (1u << q)) items[at++] = make_item(b, c, q);
+                if (keep & (1u << q)) items[at++] = make_item(b, c, q);
     }
 }
 
@@ -561,34 +635,36 @@ __device__ __forceinline__ float box_gap2(float3 ilo, float3 ihi, float3 jlo, fl
 }
 
 // Grid-stride over the items.  For an item the CTA holds up to 128 bodies
-// of the bucket (one per thread, all in one cell) and stages the neighbour
-// bucket in shared memory kTileJ bodies at a time.  Each thread then works
-// through the staged bodies 128 at a time: it collects the slots within
-// r2 < 1 of its body, then evaluates the contact law on those alone.  A
-// warp skips each staged block of 32 bodies whose bounding box is provably
-// out of reach of its own bodies' box.  One barrier pair per kTileJ staged
-// bodies lets the warps' uneven hit counts even out between barriers.
-constexpr int kTileJ = 256;
-
-__global__ void __launch_bounds__(128, 8)
+// of the bucket b (one per thread, all in one cell), stages the neighbour
+// bucket nb in shared memory 128 bodies at a time, and each thread
+// collects the tile slots within r2 < 1 of its body before evaluating the
+// contact law on those alone.  A warp skips each staged block of 32 bodies
+// whose bounding box is provably out of reach of its own bodies' box.
+// When nb is tiled too, each pair is evaluated once for both bodies: the
+// item covers nb's tiles from the chunk's own slots on (all of them when
+// nb != b; within the chunk's own tile only slots above the thread's), and
+// the staged bodies' sums are flushed with 64-bit atomics once per tile.
+__global__ void __launch_bounds__(128)
 contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                     const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
-                    unsigned int mask, long long *__restrict__ delta,
-                    const __grid_constant__ LaunchTable tab,
+                    const unsigned int *__restrict__ state, unsigned int mask,
+                    long long *__restrict__ delta, const __grid_constant__ LaunchTable tab,
                     const unsigned long long *__restrict__ items,
                     const unsigned int *__restrict__ nitems)
 {
     constexpr int kStride = 132;  // bytes per hit list row: rows start in distinct banks
-    constexpr int kBlocks = kTileJ / 32;
-    __shared__ float4 sp[kTileJ];  // x, y, z, body index (bits); NaN xyz outside the run
-    __shared__ float4 sv[kTileJ];
-    __shared__ float3 blo[kBlocks], bhi[kBlocks];  // box of each staged block of 32
+    __shared__ float4 sp[128];    // x, y, z, body index (bits); NaN xyz outside the run
+    __shared__ float4 sv[128];
+    __shared__ float3 blo[4], bhi[4];  // box of each staged block of 32
+    __shared__ unsigned int js[6][128];  // j-side sums of the staged slots (pair items)
     __shared__ unsigned char hits[128 * kStride];
     const unsigned int total = *nitems;
     const int t = threadIdx.x;
     const int lane = t & 31, warp = t >> 5;
     const float kInf = __int_as_float(0x7f800000);
     unsigned char *my = hits + t * kStride;
+#pragma unroll
+    for (int d = 0; d < 6; ++d) js[d][t] = 0u;
     for (unsigned int w = blockIdx.x; w < total; w += gridDim.x) {
         const unsigned long long it = items[w];
         const unsigned int b = (unsigned int)(it >> 37);
@@ -607,6 +683,8 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
                                           cell_of(p0.y) + (q / 3) % 3 - 1, cell_of(p0.z) + q / 9 - 1,
                                           mask);
         const unsigned int nbeg = nb ? cursor[nb - 1] : 0u, nend = cursor[nb];
+        const bool pair = (state[nb] & kTiled) != 0u;
+        const unsigned int first = nb == b ? s0 : nbeg;
         const int i = valid ? sorted[s0 + t] : -1;
         const float4 pi = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 vi = valid ? vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -617,60 +695,62 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
         warp_box(ilo, ihi);
         FixSum3 acc;
         fix_zero(acc);
-        for (unsigned int base = nbeg; base < nend; base += (unsigned int)kTileJ) {
+        for (unsigned int base = first; base < nend; base += 128u) {
             __syncthreads();  // the previous tile is consumed
-#pragma unroll
-            for (int r = 0; r < kTileJ / 128; ++r) {
-                const int slot = 128 * r + t;
-                const unsigned int u = base + (unsigned int)slot;
-                float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
-                if (u < nend) {
-                    const int j = sorted[u];
-                    if (j >= rbeg && j < rend) {
-                        const float4 q = pos[j];
-                        sp[slot] = make_float4(q.x, q.y, q.z, __int_as_float(j));
-                        sv[slot] = vel[j];
-                        lo = hi = make_float3(q.x, q.y, q.z);
-                    } else {  // another run's body, in a bucket shared by hashing: never a hit
-                        const float nan = __int_as_float(0x7fffffff);
-                        sp[slot] = make_float4(nan, nan, nan, __int_as_float(j));
-                    }
+            if (pair && base != first) flush_slot(js, t, __float_as_int(sp[t].w), delta);
+            const unsigned int u = base + (unsigned int)t;
+            float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
+            if (u < nend) {
+                const int j = sorted[u];
+                if (j >= rbeg && j < rend) {
+                    const float4 q = pos[j];
+                    sp[t] = make_float4(q.x, q.y, q.z, __int_as_float(j));
+                    sv[t] = vel[j];
+                    lo = hi = make_float3(q.x, q.y, q.z);
+                } else {  // another run's body, in a bucket shared by hashing: never a hit
+                    const float nan = __int_as_float(0x7fffffff);
+                    sp[t] = make_float4(nan, nan, nan, __int_as_float(j));
                 }
-                warp_box(lo, hi);
-                if (lane == 0) {
-                    blo[4 * r + warp] = lo;
-                    bhi[4 * r + warp] = hi;
-                }
+            }
+            warp_box(lo, hi);
+            if (lane == 0) {
+                blo[warp] = lo;
+                bhi[warp] = hi;
             }
             __syncthreads();
             if (!valid) continue;
-            const int cnt = (int)min((unsigned int)kTileJ, nend - base);
-            for (int h0 = 0; h0 < cnt; h0 += 128) {
-                int nh = 0;
-                for (int s = h0 / 32; s < h0 / 32 + 4 && 32 * s < cnt; ++s) {
-                    if (box_gap2(ilo, ihi, blo[s], bhi[s]) >= 1.0f) continue;  // warp-uniform
-                    const int k1 = min(cnt, 32 * s + 32);
-                    for (int k = 32 * s; k < k1; ++k) {
-                        const float4 pj = sp[k];
-                        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-                        if (r2 < 1.0f) my[nh++] = (unsigned char)(k - h0);
-                    }
-                }
-                for (int hh = 0; hh < nh; ++hh) {
-                    const int k = h0 + my[hh];
+            const int cnt = (int)min(128u, nend - base);
+            const int kmin = (nb == b && base == s0) ? t + 1 : 0;  // own tile: each pair once
+            int nh = 0;
+            for (int s = 0; s < 4 && 32 * s < cnt; ++s) {
+                if (box_gap2(ilo, ihi, blo[s], bhi[s]) >= 1.0f) continue;  // the same for the warp
+                const int k1 = min(cnt, 32 * s + 32);
+                for (int k = 32 * s; k < k1; ++k) {
                     const float4 pj = sp[k];
-                    const int j = __float_as_int(pj.w);
-                    if (j == i) continue;
                     const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
                     const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-                    const float c = contact_coef(select_row(j < sw, row_fe, row_si), tab.sep_test,
-                                                 dx, dy, dz, r2, vi, sv[k]) *
-                                    inv_unit;
-                    fix_add3(acc, c, dx, dy, dz);
+                    if (r2 < 1.0f && k >= kmin) my[nh++] = (unsigned char)k;
                 }
             }
+            // lanes start at different points of their lists, so that lanes
+            // with alike lists rarely hit one slot's shared sums at once
+            int h = (lane * nh) >> 5;
+            for (int n = 0; n < nh; ++n) {
+                const int k = my[h];
+                h = h + 1 == nh ? 0 : h + 1;
+                const float4 pj = sp[k];
+                const int j = __float_as_int(pj.w);  // never i: b and nb differ, or k > t
+                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+                const float c = contact_coef(select_row(j < sw, row_fe, row_si), tab.sep_test, dx,
+                                             dy, dz, r2, vi, sv[k]) *
+                                inv_unit;
+                if (pair) fix_add3_pair(acc, js, k, delta + 3 * (size_t)j, c, dx, dy, dz);
+                else fix_add3(acc, c, dx, dy, dz);
+            }
         }
+        __syncthreads();  // the last tile's j-side sums are complete
+        if (pair && first < nend) flush_slot(js, t, __float_as_int(sp[t].w), delta);
         fix_fold(acc);
         const long long ax = acc.x, ay = acc.y, az = acc.z;
         if (valid && (ax | ay | az)) {
@@ -759,12 +839,15 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     gi::grid_scatter<<<gk, 256, 0, s>>>(tab, keys, cursor, sorted);
     const unsigned int dmin = (unsigned int)tab.dense_min;
     gi::dense_check_kernel<<<gk, 256, 0, s>>>(pos, tab, keys, cursor, sorted, dmin, state, delta);
-    gi::dense_items_kernel<<<std::min((int)((m + 255) / 256), 4 * nsm), 256, 0, s>>>(
-        pos, tab, cursor, sorted, m, m - 1, dmin, state, items, nitems, tiled, ntiled);
+    gi::dense_mark_kernel<<<std::min((int)((m + 255) / 256), 4 * nsm), 256, 0, s>>>(
+        cursor, m, dmin, state, tiled, ntiled);
     gi::dense_sort_kernel<<<2 * nsm, 256, 0, s>>>(pos, cursor, sorted, tiled, ntiled);
+    const int gt = (int)std::min<size_t>((dense_bucket_capacity(bodies) + 255) / 256, 4 * (size_t)nsm);
+    gi::dense_items_kernel<<<gt, 256, 0, s>>>(pos, tab, cursor, sorted, m - 1, state, tiled, ntiled,
+                                              items, nitems);
     const dim3 gc((maxn + 7) / 8, tab.nruns);
     gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, cursor, sorted, keys, state, m - 1, delta, tab);
-    gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(pos, vel, cursor, sorted, m - 1, delta, tab,
-                                                     items, nitems);
+    gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(pos, vel, cursor, sorted, state, m - 1, delta,
+                                                     tab, items, nitems);
     return cudaGetLastError();
 }
