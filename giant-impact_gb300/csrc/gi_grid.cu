@@ -634,6 +634,12 @@ __device__ __forceinline__ float box_gap2(float3 ilo, float3 ihi, float3 jlo, fl
     return __fmaf_rn(gz, gz, __fmaf_rn(gx, gx, __fmul_rn(gy, gy)));
 }
 
+// Shared-memory position of staged slot k (0..127).  Lanes walking their
+// hit lists (ascending slots) from staggered starts read slots about 4
+// apart; this layout puts such slots in distinct banks, for the 16-byte
+// staged bodies and for the 4-byte j-side sums alike.
+__device__ __forceinline__ int swz(int k) { return ((k & 3) << 5) | (k >> 2); }
+
 // Grid-stride over the items.  For an item the CTA holds up to 128 bodies
 // of the bucket b (one per thread, all in one cell), stages the neighbour
 // bucket nb in shared memory 128 bodies at a time, and each thread
@@ -660,6 +666,7 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
     __shared__ unsigned char hits[128 * kStride];
     const unsigned int total = *nitems;
     const int t = threadIdx.x;
+    const int tz = swz(t);  // where this thread stages its slot
     const int lane = t & 31, warp = t >> 5;
     const float kInf = __int_as_float(0x7f800000);
     unsigned char *my = hits + t * kStride;
@@ -697,19 +704,19 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
         fix_zero(acc);
         for (unsigned int base = first; base < nend; base += 128u) {
             __syncthreads();  // the previous tile is consumed
-            if (pair && base != first) flush_slot(js, t, __float_as_int(sp[t].w), delta);
+            if (pair && base != first) flush_slot(js, tz, __float_as_int(sp[tz].w), delta);
             const unsigned int u = base + (unsigned int)t;
             float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
             if (u < nend) {
                 const int j = sorted[u];
                 if (j >= rbeg && j < rend) {
                     const float4 q = pos[j];
-                    sp[t] = make_float4(q.x, q.y, q.z, __int_as_float(j));
-                    sv[t] = vel[j];
+                    sp[tz] = make_float4(q.x, q.y, q.z, __int_as_float(j));
+                    sv[tz] = vel[j];
                     lo = hi = make_float3(q.x, q.y, q.z);
                 } else {  // another run's body, in a bucket shared by hashing: never a hit
                     const float nan = __int_as_float(0x7fffffff);
-                    sp[t] = make_float4(nan, nan, nan, __int_as_float(j));
+                    sp[tz] = make_float4(nan, nan, nan, __int_as_float(j));
                 }
             }
             warp_box(lo, hi);
@@ -725,18 +732,22 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
             for (int s = 0; s < 4 && 32 * s < cnt; ++s) {
                 if (box_gap2(ilo, ihi, blo[s], bhi[s]) >= 1.0f) continue;  // the same for the warp
                 const int k1 = min(cnt, 32 * s + 32);
-                for (int k = 32 * s; k < k1; ++k) {
-                    const float4 pj = sp[k];
-                    const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                    const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-                    if (r2 < 1.0f && k >= kmin) my[nh++] = (unsigned char)k;
+                for (int k = 32 * s; k < k1; k += 4) {  // swz(k + c) = 32 c + k / 4
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        if (k + c >= k1) break;
+                        const float4 pj = sp[32 * c + (k >> 2)];
+                        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+                        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+                        if (r2 < 1.0f && k + c >= kmin) my[nh++] = (unsigned char)(k + c);
+                    }
                 }
             }
             // lanes start at different points of their lists, so that lanes
             // with alike lists rarely hit one slot's shared sums at once
             int h = (lane * nh) >> 5;
             for (int n = 0; n < nh; ++n) {
-                const int k = my[h];
+                const int k = swz(my[h]);  // shared-memory position of the slot
                 h = h + 1 == nh ? 0 : h + 1;
                 const float4 pj = sp[k];
                 const int j = __float_as_int(pj.w);  // never i: b and nb differ, or k > t
@@ -750,7 +761,7 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
             }
         }
         __syncthreads();  // the last tile's j-side sums are complete
-        if (pair && first < nend) flush_slot(js, t, __float_as_int(sp[t].w), delta);
+        if (pair && first < nend) flush_slot(js, tz, __float_as_int(sp[tz].w), delta);
         fix_fold(acc);
         const long long ax = acc.x, ay = acc.y, az = acc.z;
         if (valid && (ax | ay | az)) {
