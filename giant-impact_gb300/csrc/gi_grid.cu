@@ -479,12 +479,9 @@ __device__ __forceinline__ int run_of_body(const LaunchTable &tab, int i)
     return 0;
 }
 
-// Item = bucket (27 bits) << 37 | chunk of 128 bodies (32 bits) << 5 |
-// neighbour offset (0..26).
-__device__ __forceinline__ unsigned long long make_item(unsigned int b, unsigned int c, int q)
-{
-    return ((unsigned long long)b << 37) | ((unsigned long long)c << 5) | (unsigned long long)q;
-}
+// Work item of the tiled path: x = bucket, y = neighbour bucket, z = chunk
+// of 128 of the bucket's bodies, w = run.  Carrying all four saves the
+// tile kernel a chain of dependent loads per item.
 
 // Pass 2, one thread per bucket: a dense bucket of one cell becomes tiled
 // and is listed in tiled[0 .. *ntiled).
@@ -512,7 +509,7 @@ dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ Launc
                    const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
                    unsigned int mask, const unsigned int *__restrict__ state,
                    const unsigned int *__restrict__ tiled, const unsigned int *__restrict__ ntiled,
-                   unsigned long long *__restrict__ items, unsigned int *__restrict__ nitems)
+                   uint4 *__restrict__ items, unsigned int *__restrict__ nitems)
 {
     const unsigned int total = *ntiled;
     for (unsigned int w = blockIdx.x * blockDim.x + threadIdx.x; w < total;
@@ -537,7 +534,7 @@ dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ Launc
         unsigned int at = atomicAdd(nitems, nch * nq);
         for (unsigned int c = 0; c < nch; ++c)
             for (int q = 0; q < 27; ++q)
-                if (keep & (1u << q)) items[at++] = make_item(b, c, q);
+                if (keep & (1u << q)) items[at++] = make_uint4(b, nb[q], c, (unsigned int)r);
     }
 }
 
@@ -653,9 +650,8 @@ __device__ __forceinline__ int swz(int k) { return ((k & 3) << 5) | (k >> 2); }
 __global__ void __launch_bounds__(128)
 contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                     const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
-                    const unsigned int *__restrict__ state, unsigned int mask,
-                    long long *__restrict__ delta, const __grid_constant__ LaunchTable tab,
-                    const unsigned long long *__restrict__ items,
+                    const unsigned int *__restrict__ state, long long *__restrict__ delta,
+                    const __grid_constant__ LaunchTable tab, const uint4 *__restrict__ items,
                     const unsigned int *__restrict__ nitems)
 {
     constexpr int kStride = 132;  // bytes per hit list row: rows start in distinct banks
@@ -673,22 +669,14 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
 #pragma unroll
     for (int d = 0; d < 6; ++d) js[d][t] = 0u;
     for (unsigned int w = blockIdx.x; w < total; w += gridDim.x) {
-        const unsigned long long it = items[w];
-        const unsigned int b = (unsigned int)(it >> 37);
-        const unsigned int chunk = (unsigned int)((it >> 5) & 0xffffffffull);
-        const int q = (int)(it & 31ull);
+        const uint4 it = items[w];
+        const unsigned int b = it.x, nb = it.y, chunk = it.z;
         const unsigned int bbeg = b ? cursor[b - 1] : 0u, bend = cursor[b];
         const unsigned int s0 = bbeg + 128u * chunk;
         const bool valid = s0 + (unsigned int)t < bend;
-        const int j0 = sorted[s0];  // every item's chunk holds at least one body
-        const int run = run_of_body(tab, j0);
-        const RunDev &R = tab.runs[run];
+        const RunDev &R = tab.runs[it.w];
         const int rbeg = R.offset, rend = R.offset + R.n, sw = R.offset + R.nfe;
         const float inv_unit = (float)(1.0 / tab.params[R.param].fx_unit);
-        const float4 p0 = pos[j0];
-        const unsigned int nb = bucket_of(run, cell_of(p0.x) + q % 3 - 1,
-                                          cell_of(p0.y) + (q / 3) % 3 - 1, cell_of(p0.z) + q / 9 - 1,
-                                          mask);
         const unsigned int nbeg = nb ? cursor[nb - 1] : 0u, nend = cursor[nb];
         const bool pair = (state[nb] & kTiled) != 0u;
         const unsigned int first = nb == b ? s0 : nbeg;
@@ -799,11 +787,12 @@ static size_t dense_bucket_capacity(long long bodies)
 
 // keys + sorted: `bodies` each (indexed by global body index / slot); cursor
 // and bucket state: one word per bucket each; block sums: 8192; item and
-// tiled-bucket counts (2 words); items (2 words each); tiled buckets.
+// tiled-bucket counts (2 words) and up to 3 words to align the items to 16
+// bytes; items (4 words each); tiled buckets.
 size_t gi_grid_words(long long max_end, long long bodies)
 {
-    return 2 * (size_t)max_end + 2 * (size_t)gi_grid_buckets(bodies) + 8192 + 2 +
-           2 * dense_item_capacity(bodies) + dense_bucket_capacity(bodies);
+    return 2 * (size_t)max_end + 2 * (size_t)gi_grid_buckets(bodies) + 8192 + 2 + 3 +
+           4 * dense_item_capacity(bodies) + dense_bucket_capacity(bodies);
 }
 
 cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, cudaStream_t s)
@@ -830,7 +819,8 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     unsigned int *sums = state + m;
     unsigned int *nitems = sums + 8192;
     unsigned int *ntiled = nitems + 1;
-    unsigned long long *items = reinterpret_cast<unsigned long long *>(nitems + 2);  // 8-byte aligned
+    uint4 *items = reinterpret_cast<uint4 *>((reinterpret_cast<uintptr_t>(nitems + 2) + 15) &
+                                             ~static_cast<uintptr_t>(15));
     unsigned int *tiled = reinterpret_cast<unsigned int *>(items + dense_item_capacity(bodies));
     int maxn = 0;
     for (int r = 0; r < tab.nruns; ++r) maxn = std::max(maxn, tab.runs[r].n);
@@ -858,7 +848,7 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
                                               items, nitems);
     const dim3 gc((maxn + 7) / 8, tab.nruns);
     gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, cursor, sorted, keys, state, m - 1, delta, tab);
-    gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(pos, vel, cursor, sorted, state, m - 1, delta,
-                                                     tab, items, nitems);
+    gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(pos, vel, cursor, sorted, state, delta, tab,
+                                                     items, nitems);
     return cudaGetLastError();
 }
