@@ -498,12 +498,14 @@ dense_mark_kernel(const unsigned int *__restrict__ cursor, unsigned int m, unsig
     }
 }
 
-// Pass 4, one thread per tiled bucket b: an item per (chunk of 128 of its
-// bodies, distinct non-empty neighbour bucket nb).  A pair of tiled
-// buckets is listed once, from the lower bucket number (nb >= b): its
-// item evaluates each contact pair once for both bodies.  A bucket that is
-// not tiled gets its own sums from contact_kernel, so its item adds to b's
-// bodies only.
+// Pass 4, one warp per tiled bucket b: an item per (chunk of 128 of its
+// bodies, distinct non-empty neighbour bucket nb).  Lanes 0..26 look up
+// the 27 neighbour buckets at once; a bucket that two neighbour cells
+// share is kept once.  A pair of tiled buckets is listed once, from the
+// lower bucket number (nb >= b): its item evaluates each contact pair once
+// for both bodies.  A bucket that is not tiled gets its own sums from
+// contact_kernel, so its item adds to b's bodies only.  Items are written
+// chunk by chunk, neighbours in offset order within a chunk.
 __global__ void __launch_bounds__(256)
 dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
                    const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
@@ -511,30 +513,35 @@ dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ Launc
                    const unsigned int *__restrict__ tiled, const unsigned int *__restrict__ ntiled,
                    uint4 *__restrict__ items, unsigned int *__restrict__ nitems)
 {
+    const unsigned int lane = threadIdx.x & 31u;
     const unsigned int total = *ntiled;
-    for (unsigned int w = blockIdx.x * blockDim.x + threadIdx.x; w < total;
-         w += gridDim.x * blockDim.x) {
+    const unsigned int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nwarps) {
         const unsigned int b = tiled[w];
         const unsigned int cnt = bucket_size(cursor, b);
         const int j0 = sorted[b ? cursor[b - 1] : 0u];
         const int r = run_of_body(tab, j0);
         const float4 p = pos[j0];
-        const int cx = cell_of(p.x), cy = cell_of(p.y), cz = cell_of(p.z);
-        unsigned int nb[27];
-        unsigned int keep = 0;  // bit q: offset q is the first to reach its bucket, and listed here
-        for (int q = 0; q < 27; ++q) {
-            nb[q] = bucket_of(r, cx + q % 3 - 1, cy + (q / 3) % 3 - 1, cz + q / 9 - 1, mask);
-            bool dup = false;
-            for (int u = 0; u < q; ++u) dup |= nb[u] == nb[q];
-            const bool other_side = (state[nb[q]] & kTiled) && nb[q] < b;
-            if (!dup && !other_side && bucket_size(cursor, nb[q]) > 0) keep |= 1u << q;
+        unsigned int nbq = 0xffffffffu;  // no bucket: lanes 27..31
+        if (lane < 27u)
+            nbq = bucket_of(r, cell_of(p.x) + (int)(lane % 3u) - 1, cell_of(p.y) + (int)(lane / 3u % 3u) - 1,
+                            cell_of(p.z) + (int)(lane / 9u) - 1, mask);
+        const unsigned int same = __match_any_sync(0xffffffffu, nbq);
+        bool keep = false;
+        if (lane < 27u && (same & ((1u << lane) - 1u)) == 0u) {
+            const bool other_side = (state[nbq] & kTiled) && nbq < b;
+            keep = !other_side && bucket_size(cursor, nbq) > 0u;
         }
-        const unsigned int nch = (cnt + 127u) / 128u;
-        const unsigned int nq = __popc(keep);
-        unsigned int at = atomicAdd(nitems, nch * nq);
-        for (unsigned int c = 0; c < nch; ++c)
-            for (int q = 0; q < 27; ++q)
-                if (keep & (1u << q)) items[at++] = make_uint4(b, nb[q], c, (unsigned int)r);
+        const unsigned int km = __ballot_sync(0xffffffffu, keep);
+        const unsigned int nq = __popc(km), nch = (cnt + 127u) / 128u;
+        unsigned int at = 0u;
+        if (lane == 0u) at = atomicAdd(nitems, nch * nq);
+        at = __shfl_sync(0xffffffffu, at, 0);
+        if (keep) {
+            const unsigned int rank = __popc(km & ((1u << lane) - 1u));
+            for (unsigned int c = 0; c < nch; ++c)
+                items[at + c * nq + rank] = make_uint4(b, nbq, c, (unsigned int)r);
+        }
     }
 }
 
@@ -843,7 +850,7 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     gi::dense_mark_kernel<<<std::min((int)((m + 255) / 256), 4 * nsm), 256, 0, s>>>(
         cursor, m, dmin, state, tiled, ntiled);
     gi::dense_sort_kernel<<<2 * nsm, 256, 0, s>>>(pos, cursor, sorted, tiled, ntiled);
-    const int gt = (int)std::min<size_t>((dense_bucket_capacity(bodies) + 255) / 256, 4 * (size_t)nsm);
+    const int gt = (int)std::min<size_t>((dense_bucket_capacity(bodies) + 7) / 8, 4 * (size_t)nsm);
     gi::dense_items_kernel<<<gt, 256, 0, s>>>(pos, tab, cursor, sorted, m - 1, state, tiled, ntiled,
                                               items, nitems);
     const dim3 gc((maxn + 7) / 8, tab.nruns);
