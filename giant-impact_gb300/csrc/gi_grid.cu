@@ -125,16 +125,22 @@ __global__ void __launch_bounds__(1024) scan_add(unsigned int *__restrict__ a, i
     if (i < m) a[i] += sums[blockIdx.x];
 }
 
-// After this, bucket b holds sorted[(b ? cursor[b-1] : 0) .. cursor[b]).
+// After this, bucket b holds sorted[(b ? cursor[b-1] : 0) .. cursor[b]),
+// and spos / svel hold each slot's body state: the contact passes read
+// candidates slot by slot, coalesced and without the index hop.
 __global__ void __launch_bounds__(256)
-grid_scatter(const __grid_constant__ LaunchTable tab, const unsigned int *__restrict__ keys,
-             unsigned int *__restrict__ cursor, int *__restrict__ sorted)
+grid_scatter(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+             const __grid_constant__ LaunchTable tab, const unsigned int *__restrict__ keys,
+             unsigned int *__restrict__ cursor, int *__restrict__ sorted, float4 *__restrict__ spos,
+             float4 *__restrict__ svel)
 {
     const RunDev &R = tab.runs[blockIdx.y];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < R.n; k += gridDim.x * blockDim.x) {
         const int i = R.offset + k;
         const unsigned int slot = atomicAdd(&cursor[keys[i]], 1u);
         sorted[slot] = i;
+        spos[slot] = pos[i];
+        svel[slot] = vel[i];
     }
 }
 
@@ -339,6 +345,8 @@ constexpr unsigned int kMixed = 1u, kTiled = 2u;
 // end to end, and the warp then walks that list 32 candidates at a time.
 __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos,
                                                   const float4 *__restrict__ vel,
+                                                  const float4 *__restrict__ spos,
+                                                  const float4 *__restrict__ svel,
                                                   const unsigned int *__restrict__ cursor,
                                                   const int *__restrict__ sorted, unsigned int mask,
                                                   long long *__restrict__ delta, const RunDev &R,
@@ -388,14 +396,15 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
         const unsigned int sb = __shfl_sync(0xffffffffu, beg, src);
         const unsigned int se = __shfl_sync(0xffffffffu, excl, src);
         if (t >= total) continue;
-        const int j = __ldg(&sorted[sb + (t - se)]);
-        if (j == i || j < rbeg || j >= rend) continue;
-        const float4 pj = __ldg(&pos[j]);
+        const unsigned int slot = sb + (t - se);
+        const float4 pj = __ldg(&spos[slot]);
         const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
         const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
         if (!(r2 < 1.0f)) continue;
+        const int j = __ldg(&sorted[slot]);
+        if (j == i || j < rbeg || j >= rend) continue;
         if (!have_vi) { vi = __ldg(&vel[i]); have_vi = true; }
-        const float4 vj = __ldg(&vel[j]);
+        const float4 vj = __ldg(&svel[slot]);
         const float c =
             contact_coef(select_row(j < sw, row_fe, row_si), sep_test, dx, dy, dz, r2, vi, vj) *
             inv_unit;
@@ -426,6 +435,7 @@ __device__ __forceinline__ unsigned int bucket_size(const unsigned int *__restri
 // to contact_tile_kernel.
 __global__ void __launch_bounds__(256)
 contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+               const float4 *__restrict__ spos, const float4 *__restrict__ svel,
                const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
                const unsigned int *__restrict__ keys, const unsigned int *__restrict__ state,
                unsigned int mask, long long *__restrict__ delta,
@@ -437,8 +447,8 @@ contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
     if (k >= R.n) return;  // whole warp leaves together
     const int i = R.offset + k;
     if (state[__ldg(&keys[i])] & kTiled) return;
-    contact_body_warp(pos, vel, cursor, sorted, mask, delta, R, tab.params[R.param], tab.sep_test,
-                      blockIdx.y, i, lane);
+    contact_body_warp(pos, vel, spos, svel, cursor, sorted, mask, delta, R, tab.params[R.param],
+                      tab.sep_test, blockIdx.y, i, lane);
 }
 
 // Pass 1, one thread per body of the run blockIdx.y: for bodies of dense
@@ -567,9 +577,10 @@ constexpr unsigned int kSortCap = 8192;
 // changes; the contact sums are exact integer sums, so the forces do not
 // depend on it.  A bucket above kSortCap keeps its order.
 __global__ void __launch_bounds__(256)
-dense_sort_kernel(const float4 *__restrict__ pos, const unsigned int *__restrict__ cursor,
-                  int *__restrict__ sorted, const unsigned int *__restrict__ tiled,
-                  const unsigned int *__restrict__ ntiled)
+dense_sort_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+                  const unsigned int *__restrict__ cursor, int *__restrict__ sorted,
+                  float4 *__restrict__ spos, float4 *__restrict__ svel,
+                  const unsigned int *__restrict__ tiled, const unsigned int *__restrict__ ntiled)
 {
     __shared__ int sidx[kSortCap];
     __shared__ unsigned char skey[kSortCap];
@@ -604,8 +615,13 @@ dense_sort_kernel(const float4 *__restrict__ pos, const unsigned int *__restrict
             cnt[2 * lane + 1] = excl + c0;
         }
         __syncthreads();
-        for (unsigned int u = threadIdx.x; u < n; u += blockDim.x)
-            sorted[beg + atomicAdd(&cnt[skey[u]], 1u)] = sidx[u];
+        for (unsigned int u = threadIdx.x; u < n; u += blockDim.x) {
+            const int j = sidx[u];
+            const unsigned int slot = beg + atomicAdd(&cnt[skey[u]], 1u);
+            sorted[slot] = j;
+            spos[slot] = pos[j];
+            svel[slot] = vel[j];
+        }
     }
 }
 
@@ -655,7 +671,7 @@ __device__ __forceinline__ int swz(int k) { return ((k & 3) << 5) | (k >> 2); }
 // nb != b; within the chunk's own tile only slots above the thread's), and
 // the staged bodies' sums are flushed with 64-bit atomics once per tile.
 __global__ void __launch_bounds__(128)
-contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
+contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ svel,
                     const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
                     const unsigned int *__restrict__ state, long long *__restrict__ delta,
                     const __grid_constant__ LaunchTable tab, const uint4 *__restrict__ items,
@@ -688,8 +704,8 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
         const bool pair = (state[nb] & kTiled) != 0u;
         const unsigned int first = nb == b ? s0 : nbeg;
         const int i = valid ? sorted[s0 + t] : -1;
-        const float4 pi = valid ? pos[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-        const float4 vi = valid ? vel[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 pi = valid ? spos[s0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 vi = valid ? svel[s0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
         const PairRow row_fe = pair_row(tab.params[R.param], i < sw, true);
         const PairRow row_si = pair_row(tab.params[R.param], i < sw, false);
         float3 ilo = valid ? make_float3(pi.x, pi.y, pi.z) : make_float3(kInf, kInf, kInf);
@@ -705,9 +721,9 @@ contact_tile_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ v
             if (u < nend) {
                 const int j = sorted[u];
                 if (j >= rbeg && j < rend) {
-                    const float4 q = pos[j];
+                    const float4 q = spos[u];
                     sp[tz] = make_float4(q.x, q.y, q.z, __int_as_float(j));
-                    sv[tz] = vel[j];
+                    sv[tz] = svel[u];
                     lo = hi = make_float3(q.x, q.y, q.z);
                 } else {  // another run's body, in a bucket shared by hashing: never a hit
                     const float nan = __int_as_float(0x7fffffff);
@@ -792,14 +808,15 @@ static size_t dense_bucket_capacity(long long bodies)
     return (size_t)bodies / gi::kDenseFloor + 1;
 }
 
-// keys + sorted: `bodies` each (indexed by global body index / slot); cursor
-// and bucket state: one word per bucket each; block sums: 8192; item and
+// Slot-ordered positions and velocities (float4, 8 words per slot); keys
+// (indexed by global body index) and sorted (by slot): max_end words each;
+// cursor and bucket state: one word per bucket each; block sums: 8192; item and
 // tiled-bucket counts (2 words) and up to 3 words to align the items to 16
 // bytes; items (4 words each); tiled buckets.
 size_t gi_grid_words(long long max_end, long long bodies)
 {
-    return 2 * (size_t)max_end + 2 * (size_t)gi_grid_buckets(bodies) + 8192 + 2 + 3 +
-           4 * dense_item_capacity(bodies) + dense_bucket_capacity(bodies);
+    return 8 * (size_t)bodies + 2 * (size_t)max_end + 2 * (size_t)gi_grid_buckets(bodies) + 8192 +
+           2 + 3 + 4 * dense_item_capacity(bodies) + dense_bucket_capacity(bodies);
 }
 
 cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, cudaStream_t s)
@@ -819,9 +836,12 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     if (tab.nruns <= 0) return cudaSuccess;
     const unsigned int m = gi_grid_buckets(bodies);
     if (m > 1024u * 8192u) return cudaErrorInvalidValue;
-    unsigned int *keys = work;
-    int *sorted = reinterpret_cast<int *>(work + max_end);
-    unsigned int *cursor = work + 2 * (size_t)max_end;
+    if (reinterpret_cast<uintptr_t>(work) & 15u) return cudaErrorInvalidValue;
+    float4 *spos = reinterpret_cast<float4 *>(work);
+    float4 *svel = spos + bodies;
+    unsigned int *keys = work + 8 * (size_t)bodies;
+    int *sorted = reinterpret_cast<int *>(keys + max_end);
+    unsigned int *cursor = keys + 2 * (size_t)max_end;
     unsigned int *state = cursor + m;
     unsigned int *sums = state + m;
     unsigned int *nitems = sums + 8192;
@@ -844,18 +864,19 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     gi::scan_blocks<<<sb, 1024, 0, s>>>(cursor, (int)m, sums);
     gi::scan_sums<<<1, 1024, 0, s>>>(sums, sb);
     gi::scan_add<<<sb, 1024, 0, s>>>(cursor, (int)m, sums);
-    gi::grid_scatter<<<gk, 256, 0, s>>>(tab, keys, cursor, sorted);
+    gi::grid_scatter<<<gk, 256, 0, s>>>(pos, vel, tab, keys, cursor, sorted, spos, svel);
     const unsigned int dmin = (unsigned int)tab.dense_min;
     gi::dense_check_kernel<<<gk, 256, 0, s>>>(pos, tab, keys, cursor, sorted, dmin, state, delta);
     gi::dense_mark_kernel<<<std::min((int)((m + 255) / 256), 4 * nsm), 256, 0, s>>>(
         cursor, m, dmin, state, tiled, ntiled);
-    gi::dense_sort_kernel<<<2 * nsm, 256, 0, s>>>(pos, cursor, sorted, tiled, ntiled);
+    gi::dense_sort_kernel<<<2 * nsm, 256, 0, s>>>(pos, vel, cursor, sorted, spos, svel, tiled, ntiled);
     const int gt = (int)std::min<size_t>((dense_bucket_capacity(bodies) + 7) / 8, 4 * (size_t)nsm);
     gi::dense_items_kernel<<<gt, 256, 0, s>>>(pos, tab, cursor, sorted, m - 1, state, tiled, ntiled,
                                               items, nitems);
     const dim3 gc((maxn + 7) / 8, tab.nruns);
-    gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, cursor, sorted, keys, state, m - 1, delta, tab);
-    gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(pos, vel, cursor, sorted, state, delta, tab,
+    gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, spos, svel, cursor, sorted, keys, state, m - 1,
+                                          delta, tab);
+    gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(spos, svel, cursor, sorted, state, delta, tab,
                                                      items, nitems);
     return cudaGetLastError();
 }

@@ -13,7 +13,7 @@
 //     cudaFree can synchronise the whole device, holding up every stream.
 // For them, gi_forces_collision_noalloc computes the same forces with all of
 // its scratch in one statically allocated device array, g_noalloc_scratch,
-// of GI_NOALLOC_BYTES (10 MiB).  Every GPU that loads the library holds that
+// of GI_NOALLOC_BYTES (12 MiB).  Every GPU that loads the library holds that
 // array until the process exits.  The array limits a call to
 // GI_NOALLOC_MAX_BODIES (32,768) bodies; larger calls are refused.
 //
@@ -32,7 +32,7 @@
 
 #include "gi_internal.h"
 
-#define GI_NOALLOC_BYTES (10u << 20)
+#define GI_NOALLOC_BYTES (12u << 20)
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GI_NOALLOC_BYTES];
 

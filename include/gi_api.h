@@ -220,7 +220,7 @@ int gi_move_damped_separate(float *pos, float *vel, const float *force,
  * the budget), and step loops that must not stall on the device-wide
  * synchronisation cudaMalloc / cudaFree can cause.  It has no counterpart in
  * the reference, which allocates nothing beyond its three body arrays.
- * All scratch lives in one static device array of 10 MiB that every GPU
+ * All scratch lives in one static device array of 12 MiB that every GPU
  * loading the library holds until exit, so a call takes at most
  * GI_NOALLOC_MAX_BODIES bodies (larger n returns GI_ERR_BAD_SIZE).  The
  * first call on a device looks the array up (cudaGetSymbolAddress); make it
