@@ -158,6 +158,7 @@ static int to_device_params(const gi_pair_params &p, PairDev &d)
                          (double)std::fabs(d.KRin[t])});
     }
     d.fx_unit = std::ldexp(2.0 * gmax + kmax, -40);
+    d.inv_unit = (float)(1.0 / d.fx_unit);
     return GI_OK;
 }
 

@@ -378,37 +378,58 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
     const unsigned int total = __shfl_sync(0xffffffffu, incl, 31);
     const unsigned int excl = incl - cnt;
 
-    const float inv_unit = (float)(1.0 / P.fx_unit);
+    const float inv_unit = P.inv_unit;
     const PairRow row_fe = pair_row(P, i < sw, true), row_si = pair_row(P, i < sw, false);
-    float4 vi = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool have_vi = false;
+    const float4 vi = __ldg(&vel[i]);
+    const float nan = __int_as_float(0x7fffffff);
     FixSum3 acc;
     fix_zero(acc);
-    for (unsigned int base = 0; base < total; base += 32) {
-        const unsigned int t = base + lane;
+    // 64 candidates a pass, two per lane, so that each lane has two
+    // independent loads in flight
+    for (unsigned int base = 0; base < total; base += 64) {
+        unsigned int t[2] = {base + lane, base + 32 + lane};
         // the lane whose range [excl, incl) holds t: last lane with excl <= t
-        int src = 0;
+        int src[2] = {0, 0};
 #pragma unroll
         for (int step = 16; step > 0; step >>= 1) {
-            const unsigned int e = __shfl_sync(0xffffffffu, excl, src + step);
-            if (src + step < 32 && e <= t) src += step;
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                const unsigned int e = __shfl_sync(0xffffffffu, excl, src[u] + step);
+                if (src[u] + step < 32 && e <= t[u]) src[u] += step;
+            }
         }
-        const unsigned int sb = __shfl_sync(0xffffffffu, beg, src);
-        const unsigned int se = __shfl_sync(0xffffffffu, excl, src);
-        if (t >= total) continue;
-        const unsigned int slot = sb + (t - se);
-        const float4 pj = __ldg(&spos[slot]);
-        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-        if (!(r2 < 1.0f)) continue;
-        const int j = __ldg(&sorted[slot]);
-        if (j == i || j < rbeg || j >= rend) continue;
-        if (!have_vi) { vi = __ldg(&vel[i]); have_vi = true; }
-        const float4 vj = __ldg(&svel[slot]);
-        const float c =
-            contact_coef(select_row(j < sw, row_fe, row_si), sep_test, dx, dy, dz, r2, vi, vj) *
-            inv_unit;
-        fix_add3(acc, c, dx, dy, dz);
+        unsigned int slot[2];
+        float4 pj[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const unsigned int sb = __shfl_sync(0xffffffffu, beg, src[u]);
+            const unsigned int se = __shfl_sync(0xffffffffu, excl, src[u]);
+            slot[u] = sb + (t[u] - se);
+            pj[u] = t[u] < total ? __ldg(&spos[slot[u]]) : make_float4(nan, nan, nan, 0.f);
+        }
+        float dx[2], dy[2], dz[2], r2[2];
+        int j[2] = {i, i};
+        float4 vj[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            dx[u] = pj[u].x - pi.x;
+            dy[u] = pj[u].y - pi.y;
+            dz[u] = pj[u].z - pi.z;
+            r2[u] = __fmaf_rn(dz[u], dz[u], __fmaf_rn(dx[u], dx[u], __fmul_rn(dy[u], dy[u])));
+            if (r2[u] < 1.0f) {
+                j[u] = __ldg(&sorted[slot[u]]);
+                vj[u] = __ldg(&svel[slot[u]]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            // not a hit (j stays i), the body itself, or another run's body
+            if (j[u] == i || j[u] < rbeg || j[u] >= rend) continue;
+            const float c = contact_coef(select_row(j[u] < sw, row_fe, row_si), sep_test, dx[u],
+                                         dy[u], dz[u], r2[u], vi, vj[u]) *
+                            inv_unit;
+            fix_add3(acc, c, dx[u], dy[u], dz[u]);
+        }
     }
     fix_fold(acc);
     long long ax = acc.x, ay = acc.y, az = acc.z;
@@ -699,7 +720,7 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
         const bool valid = s0 + (unsigned int)t < bend;
         const RunDev &R = tab.runs[it.w];
         const int rbeg = R.offset, rend = R.offset + R.n, sw = R.offset + R.nfe;
-        const float inv_unit = (float)(1.0 / tab.params[R.param].fx_unit);
+        const float inv_unit = tab.params[R.param].inv_unit;
         const unsigned int nbeg = nb ? cursor[nb - 1] : 0u, nend = cursor[nb];
         const bool pair = (state[nb] & kTiled) != 0u;
         const unsigned int first = nb == b ? s0 : nbeg;

@@ -36,6 +36,7 @@ struct PairDev {
     float KRin[3];       // reduced stiffness, inner band
     float Tband[3];      // r >= ShellBreak(1)  <=>  r2 >= Tband
     float Tmid[3];       // r >= ShellBreakFeSi2 <=> r2 >= Tmid (= Tband otherwise)
+    float inv_unit;      // (float)(1 / fx_unit), the scale of a pair term into fixed point
 };
 
 struct RunDev {
