@@ -342,7 +342,8 @@ constexpr unsigned int kMixed = 1u, kTiled = 2u;
 // Contact correction of body i (run r) by one warp.  Lanes 0..26 look up
 // the 27 neighbour buckets at once (one memory round trip; a bucket that
 // two neighbour cells share is kept once), a warp scan lays their bodies
-// end to end, and the warp then walks that list 32 candidates at a time.
+// end to end, and the warp then filters that list 64 candidates at a time
+// into the shared hit list q (96 slots), which it evaluates 32 at a time.
 __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos,
                                                   const float4 *__restrict__ vel,
                                                   const float4 *__restrict__ spos,
@@ -351,7 +352,7 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
                                                   const int *__restrict__ sorted, unsigned int mask,
                                                   long long *__restrict__ delta, const RunDev &R,
                                                   const PairDev &P, int sep_test, int r, int i,
-                                                  int lane)
+                                                  int lane, unsigned int *q)
 {
     const int rbeg = R.offset, rend = R.offset + R.n, sw = R.offset + R.nfe;
     const float4 pi = __ldg(&pos[i]);
@@ -382,10 +383,29 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
     const PairRow row_fe = pair_row(P, i < sw, true), row_si = pair_row(P, i < sw, false);
     const float4 vi = __ldg(&vel[i]);
     const float nan = __int_as_float(0x7fffffff);
+    const unsigned int below = (1u << lane) - 1u;
     FixSum3 acc;
     fix_zero(acc);
+    // Contact law on queued hits, one per lane (lanes >= n idle): slots
+    // q[base .. base + n).
+    const auto drain = [&](unsigned int base, unsigned int n) {
+        if ((unsigned int)lane >= n) return;
+        const unsigned int slot = q[base + lane];
+        const int j = __ldg(&sorted[slot]);
+        if (j == i || j < rbeg || j >= rend) return;  // the body itself, or another run's body
+        const float4 pj = __ldg(&spos[slot]), vj = __ldg(&svel[slot]);
+        const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
+        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+        const float c =
+            contact_coef(select_row(j < sw, row_fe, row_si), sep_test, dx, dy, dz, r2, vi, vj) *
+            inv_unit;
+        fix_add3(acc, c, dx, dy, dz);
+    };
     // 64 candidates a pass, two per lane, so that each lane has two
-    // independent loads in flight
+    // independent loads in flight.  Slots within r2 < 1 are queued in the
+    // warp's shared list q and evaluated 32 at a time, so the contact law
+    // runs on full warps however sparse the hits.
+    unsigned int nq = 0;  // queued hits, the same in every lane
     for (unsigned int base = 0; base < total; base += 64) {
         unsigned int t[2] = {base + lane, base + 32 + lane};
         // the lane whose range [excl, incl) holds t: last lane with excl <= t
@@ -407,30 +427,23 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
             slot[u] = sb + (t[u] - se);
             pj[u] = t[u] < total ? __ldg(&spos[slot[u]]) : make_float4(nan, nan, nan, 0.f);
         }
-        float dx[2], dy[2], dz[2], r2[2];
-        int j[2] = {i, i};
-        float4 vj[2];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-            dx[u] = pj[u].x - pi.x;
-            dy[u] = pj[u].y - pi.y;
-            dz[u] = pj[u].z - pi.z;
-            r2[u] = __fmaf_rn(dz[u], dz[u], __fmaf_rn(dx[u], dx[u], __fmul_rn(dy[u], dy[u])));
-            if (r2[u] < 1.0f) {
-                j[u] = __ldg(&sorted[slot[u]]);
-                vj[u] = __ldg(&svel[slot[u]]);
-            }
+            const float dx = pj[u].x - pi.x, dy = pj[u].y - pi.y, dz = pj[u].z - pi.z;
+            const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+            const bool hit = r2 < 1.0f;
+            const unsigned int m = __ballot_sync(0xffffffffu, hit);
+            if (hit) q[nq + __popc(m & below)] = slot[u];
+            nq += __popc(m);
         }
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            // not a hit (j stays i), the body itself, or another run's body
-            if (j[u] == i || j[u] < rbeg || j[u] >= rend) continue;
-            const float c = contact_coef(select_row(j[u] < sw, row_fe, row_si), sep_test, dx[u],
-                                         dy[u], dz[u], r2[u], vi, vj[u]) *
-                            inv_unit;
-            fix_add3(acc, c, dx[u], dy[u], dz[u]);
+        __syncwarp();
+        while (nq >= 32u) {
+            nq -= 32u;
+            drain(nq, 32u);
+            __syncwarp();  // the slots are read before the queue refills
         }
     }
+    drain(0u, nq);
     fix_fold(acc);
     long long ax = acc.x, ay = acc.y, az = acc.z;
 #pragma unroll
@@ -462,6 +475,7 @@ contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                unsigned int mask, long long *__restrict__ delta,
                const __grid_constant__ LaunchTable tab)
 {
+    __shared__ unsigned int hitq[8][96];  // per warp: queued hit slots (up to 31 + 64)
     const RunDev &R = tab.runs[blockIdx.y];
     const int lane = threadIdx.x & 31;
     const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -469,7 +483,7 @@ contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
     const int i = R.offset + k;
     if (state[__ldg(&keys[i])] & kTiled) return;
     contact_body_warp(pos, vel, spos, svel, cursor, sorted, mask, delta, R, tab.params[R.param],
-                      tab.sep_test, blockIdx.y, i, lane);
+                      tab.sep_test, blockIdx.y, i, lane, hitq[threadIdx.x >> 5]);
 }
 
 // Pass 1, one thread per body of the run blockIdx.y: for bodies of dense
