@@ -16,7 +16,8 @@
 //      with the larger index under the one with the smaller index (one
 //      atomicCAS on a root), so a tree's root is its smallest member: the
 //      reference's group number;
-//   3. flatten: group[i] = root of i; sizes by atomicAdd;
+//   3. flatten: group[i] = root of i (found without writes, so that no
+//      thread overwrites a final root); sizes by atomicAdd;
 //   4. pick: Earth = largest group, smallest name on a tie (the reference's
 //      first strict maximum); Moon = largest of the others; both by a 64-bit
 //      atomicMax of (size << 32 | ~name);
@@ -93,6 +94,18 @@ __device__ __forceinline__ int find_root(int *parent, int x)
     }
 }
 
+// Root of x without writes.  The flatten pass writes every body's final
+// root; a path-halving write from another thread, based on a parent read
+// before that write, could replace it with an intermediate ancestor.
+__device__ __forceinline__ int find_root_ro(const int *parent, int x)
+{
+    for (;;) {
+        const int p = __ldcg(&parent[x]);
+        if (p == x) return x;
+        x = p;
+    }
+}
+
 __device__ __forceinline__ bool link(int *parent, int a, int b)
 {
     for (int t = 0; t < kClusterTries; ++t) {
@@ -150,7 +163,7 @@ cluster_flatten(int *parent, int n, int *__restrict__ size, int *__restrict__ ng
 {
     int roots = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int r = find_root(parent, i);
+        const int r = find_root_ro(parent, i);
         __stcg(&parent[i], r);
         atomicAdd(&size[r], 1);
         roots += r == i;
