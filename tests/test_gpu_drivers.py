@@ -57,6 +57,23 @@ def test_groups_match_reference_loop(gi, orc, torch_cuda, case):
     ctx.close()
 
 
+def test_groups_repeat_on_percolating_gas(gi, orc, torch_cuda):
+    """Gas near the percolation density gives long chains, where concurrent
+    root walks meet most often: every repeat names every body's group as the
+    reference loop does."""
+    torch = torch_cuda
+    ctx = gi.Context(0)
+    for seed in range(20, 28):
+        pos = _gas(seed, 4000, 27.0)
+        n = len(pos)
+        bounds = [n // 5, 2 * n // 5, 3 * n // 5]
+        want = orc.groups_ref(pos)
+        for _ in range(4):
+            em, g, sc = _groups(gi, torch, ctx, pos, bounds)
+            _check_against(em, g, sc, want, orc, bounds)
+    ctx.close()
+
+
 def _gas(seed, n, box):
     rng = np.random.default_rng(seed)
     pos = np.zeros((n, 4), np.float32)
