@@ -705,7 +705,7 @@ __device__ __forceinline__ int swz(int k) { return ((k & 3) << 5) | (k >> 2); }
 // item covers nb's tiles from the chunk's own slots on (all of them when
 // nb != b; within the chunk's own tile only slots above the thread's), and
 // the staged bodies' sums are flushed with 64-bit atomics once per tile.
-__global__ void __launch_bounds__(128, 8)
+__global__ void __launch_bounds__(128)
 contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ svel,
                     const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
                     const unsigned int *__restrict__ state, long long *__restrict__ delta,
@@ -911,16 +911,6 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     const dim3 gc((maxn + 7) / 8, tab.nruns);
     gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, spos, svel, cursor, sorted, keys, state, m - 1,
                                           delta, tab);
-    // Eight CTAs of the tiled kernel fit an SM only with the largest shared-memory carveout.
-    static bool carveout_set[64] = {};
-    int dev = 0;
-    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && !carveout_set[dev]) {
-        e = cudaFuncSetAttribute(gi::contact_tile_kernel,
-                                 cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 (int)cudaSharedmemCarveoutMaxShared);
-        if (e != cudaSuccess) return e;
-        carveout_set[dev] = true;
-    }
     gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(spos, svel, cursor, sorted, state, delta, tab,
                                                      items, nitems);
     return cudaGetLastError();
