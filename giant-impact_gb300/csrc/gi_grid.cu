@@ -7,30 +7,32 @@
 //   1. grid: every body gets the cell floor(x), floor(y), floor(z) (cell size
 //      D = 1, so two bodies within r < 1 are in the same or adjacent cells),
 //      hashed with its run into M = 2^k buckets; a counting sort (histogram,
-//      exclusive scan, scatter) lists the bodies of each bucket.
-//   2. contact kernel: one warp per body scans the buckets of its 27
-//      neighbour cells; for each j of the same run with FP32 r2 < 1 it adds
-//          contact force of the reference law  -  the clamped far-field term
-//      the all-pairs pass added for that pair.  Band and K/KR choices use the
-//      reference's FP32 r2 and dp.dv (bit-identical decisions).
-//   3. each pair's correction is evaluated in FP32 and summed in 64-bit
-//      fixed point (unit = (2 Gmax + Kmax) 2^-40 per pair table): integer
-//      adds are exact, so the sum does not depend on the order in which
-//      bodies landed in buckets or lanes found them, and the result is
-//      bit-reproducible.
+//      exclusive scan, scatter) lists the bodies of each bucket and copies
+//      their state into slot order.
+//   2. contact law: for each j of the same run with FP32 r2 < 1, the pass
+//      adds the contact force of the reference law minus the clamped
+//      far-field term the all-pairs pass added for that pair.  Band and K/KR
+//      choices use the reference's FP32 r2 and dp.dv (bit-identical
+//      decisions).
+//   3. each pair's correction is evaluated in FP32, rounded to an integer
+//      of the fixed point (unit = (2 Gmax + Kmax) 2^-40 per pair table) and
+//      summed in 64 bits: integer adds are exact, so the sum does not depend
+//      on the order in which bodies landed in buckets or lanes found them,
+//      and the result is bit-reproducible.
 // The all-pairs epilogue adds the correction before its single rounding.
 //
-// Dense buckets (at least gi_options.dense_min bodies, 256 by default, e.g.
-// an interpenetrating collision remnant with thousands of contacts per
-// body) whose bodies all share one cell go through a tiled path instead: a
-// work item is (bucket, chunk of 128 of its bodies, one neighbour bucket);
-// its CTA stages that neighbour bucket in shared memory 128 bodies at a
-// time, each thread filters the tile into a hit list and evaluates the
-// contact law on the hits only, and the item's sums are added to the
-// body's correction with 64-bit integer atomics.  The candidate set, the
-// pair law and the fixed-point terms are those of the warp path and
-// integer addition is exact, so the corrections are bit-identical
-// whichever path a body takes.
+// Two passes share the bodies.  contact_kernel gives one warp to each body
+// of an ordinary cell.  Dense buckets (at least gi_options.dense_min bodies,
+// 256 by default, e.g. an interpenetrating collision remnant with thousands
+// of contacts per body) whose bodies all share one cell are sorted by
+// sub-cell and go through contact_tile_kernel: a work item is (bucket,
+// neighbour bucket, chunk of 128 of its bodies); its CTA stages the
+// neighbour bucket in shared memory 128 bodies at a time, each thread
+// filters the tile into a hit list and evaluates the law on the hits only,
+// and a pair of two dense cells is evaluated once for both bodies.  The
+// candidate sets, the pair law and the fixed-point terms are the same on
+// both paths and integer addition is exact, so the corrections are
+// bit-identical whichever path a body takes.
 #include <algorithm>
 
 #include "gi_force_impl.cuh"
