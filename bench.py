@@ -73,6 +73,11 @@ def args_parse():
                     help="untimed steps before timing (times the impact's contact phase)")
     ap.add_argument("--dense-min", type=int, default=0,
                     help="contact pass: bucket size for the tiled path (0 = library default)")
+    ap.add_argument("--no-collision", action="store_true",
+                    help="skip the collision-phase section of the default run")
+    ap.add_argument("--collision-advance", type=int, default=6000,
+                    help="steps from the timed state into the collision phase")
+    ap.add_argument("--collision-steps", type=int, default=20)
     ap.add_argument("--no-large", action="store_true")
     ap.add_argument("--large-steps", type=int, default=4)
     ap.add_argument("--study", choices=["drift", "precision"], default=None,
@@ -484,6 +489,44 @@ def _pingpong(torch, pos, vel):
              torch.empty((n, 4), dtype=torch.float32, device="cuda"))]
 
 
+def collision_section(torch, ctx, flush, pos_d, vel_d, run, p, a):
+    """The same impact a.collision_advance steps later, when the merged bodies
+    interpenetrate (about 3,000 contacts per body) and the contact passes
+    cost as much as the far field: most of a 20,000-step impact is spent in
+    this phase.  Untimed advance, 3 warm-up steps, then a.collision_steps
+    steps timed one by one with CUDA events, L2 flushed between them."""
+    n = pos_d.shape[0]
+    bufs = [(pos_d.clone(), vel_d.clone()), (torch.empty_like(pos_d), torch.empty_like(vel_d))]
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    ctx.step(bufs[0][0].data_ptr(), bufs[0][1].data_ptr(), [run], p, a.collision_advance, s)
+
+    def one(k):
+        (pa, va), (pb, vb) = bufs[k % 2], bufs[(k + 1) % 2]
+        ctx.step_pingpong(pa.data_ptr(), va.data_ptr(), pb.data_ptr(), vb.data_ptr(), [run], p, 1, s)
+
+    for k in range(3):
+        one(k)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(a.collision_steps)]
+    for k in range(a.collision_steps):
+        flush.fill_(float(k))
+        evs[k][0].record(stream)
+        one(3 + k)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    ms = sum(step_ms) / len(step_ms)
+    dp, dv = bufs[(3 + a.collision_steps) % 2]
+    return {"advance_steps": a.collision_advance, "steps": a.collision_steps, "ms_per_step": ms,
+            "value": n * (n - 1) / (ms * 1e-3), "unit": "interactions/s",
+            "step_ms_min_max": [min(step_ms), max(step_ms)],
+            "state_finite": bool(torch.isfinite(dp).all().item() and torch.isfinite(dv).all().item()),
+            "what": "fused steps (far field + both contact passes + grid) of the config-2 impact "
+                    "after the advance, from the timed state"}
+
+
 def large_n_section(gi, torch, wl, ctx, peak_sustained, a):
     """One 1,153,434-body impact (1,048,576 + 104,858, the precision-study
     state): the fused step autotuned for this N, per-step CUDA events, L2
@@ -845,6 +888,7 @@ def run_ours(a):
         refgpu = None
         if not a.no_ref_gpu:
             refgpu = ref_gpu_baseline(gi, orc, torch, pos, vel, nfe, p)
+        collision = None if a.no_collision else collision_section(torch, ctx, flush, dp, dv, run, p, a)
         large = None if a.no_large else large_n_section(gi, torch, wl, ctx, peak_sustained, a)
         sweep = None if a.no_sweep else sweep_section(gi, torch, wl, a)
         serve = None if a.no_serve else serve_section(gi, torch, wl, a)
@@ -862,7 +906,7 @@ def run_ours(a):
                        "l2": "flushed between timed steps (256 MB write, outside the events)",
                        "parallelism": f"replicas x{world}"},
             "fp32_tflops": achieved, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "ref_gpu": refgpu, "large_n": large, "sweep": sweep, "serve": serve, "clocks": clk, "gpu_launches": 12 * a.steps,
+            "ref_gpu": refgpu, "collision_phase": collision, "large_n": large, "sweep": sweep, "serve": serve, "clocks": clk, "gpu_launches": 12 * a.steps,
             "wall_s_timed_region": t_wall, "state_finite": state_ok,
             "step_ms_min_max": [min(step_ms), max(step_ms)],
         }
