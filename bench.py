@@ -617,7 +617,7 @@ def study_drift(a):
     import oracle as orc
     steps = a.study_steps or 20000
     every = a.study_every
-    ctx = gi.Context(0)
+    ctx = gi.Context(0, dense_min=a.dense_min)
     pos, vel, nfe = make_workload(gi, torch, wl, 2, a.settle_steps)
     n = len(pos)
     kr = 1.0 if a.conservative else None  # KR = K: the contact law is conservative
@@ -627,7 +627,7 @@ def study_drift(a):
         m["sd_fe"], m["sd_si"])
     run = wl.run_desc(gi, 0, n, nfe)
     out = {"study": "drift", "workload": "plain two-body impact, 66,000 bodies, dt 1e-3",
-           "steps": steps, "every": every,
+           "steps": steps, "every": every, "dense_min": a.dense_min or 256,
            "material": "KR = K (conservative control)" if kr is not None else "config 2"}
     # this library: fused step, config units
     dp, dv = torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda()
