@@ -527,8 +527,17 @@ __device__ __forceinline__ int run_of_body(const LaunchTable &tab, int i)
 }
 
 // Work item of the tiled path: x = bucket, y = neighbour bucket, z = chunk
-// of 128 of the bucket's bodies, w = run.  Carrying all four saves the
-// tile kernel a chain of dependent loads per item.
+// of 128 of the bucket's bodies, w = run | cost class << 8.  Carrying all of
+// it saves the tile kernel a chain of dependent loads per item.  The cost
+// class is the number of 128-body tiles the item stages, minus one, capped
+// at kItemClasses - 1.
+constexpr unsigned int kItemClasses = 16;
+
+// Counters of the tiled path, in one block cleared per pass: item count,
+// tiled-bucket count, queue head, then the items per cost class and the
+// fill of each class while ordering.
+constexpr int kCtrItems = 0, kCtrTiled = 1, kCtrHead = 2, kCtrClass = 4,
+              kCtrFill = 4 + (int)kItemClasses, kCtrWords = 4 + 2 * (int)kItemClasses;
 
 // Pass 2, one thread per bucket: a dense bucket of one cell becomes tiled
 // and is listed in tiled[0 .. *ntiled).
@@ -557,9 +566,11 @@ __global__ void __launch_bounds__(256)
 dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
                    const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
                    unsigned int mask, const unsigned int *__restrict__ state,
-                   const unsigned int *__restrict__ tiled, const unsigned int *__restrict__ ntiled,
-                   uint4 *__restrict__ items, unsigned int *__restrict__ nitems)
+                   const unsigned int *__restrict__ tiled, unsigned int *__restrict__ ctr,
+                   uint4 *__restrict__ items)
 {
+    const unsigned int *ntiled = ctr + kCtrTiled;
+    unsigned int *nitems = ctr + kCtrItems;
     const unsigned int lane = threadIdx.x & 31u;
     const unsigned int total = *ntiled;
     const unsigned int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -586,9 +597,39 @@ dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ Launc
         at = __shfl_sync(0xffffffffu, at, 0);
         if (keep) {
             const unsigned int rank = __popc(km & ((1u << lane) - 1u));
-            for (unsigned int c = 0; c < nch; ++c)
-                items[at + c * nq + rank] = make_uint4(b, nbq, c, (unsigned int)r);
+            const unsigned int bbeg = b ? cursor[b - 1] : 0u;
+            const unsigned int nbeg = nbq ? cursor[nbq - 1] : 0u, nend = cursor[nbq];
+            for (unsigned int c = 0; c < nch; ++c) {
+                const unsigned int first = nbq == b ? bbeg + 128u * c : nbeg;
+                const unsigned int cls = min((nend - first + 127u) / 128u, kItemClasses) - 1u;
+                items[at + c * nq + rank] = make_uint4(b, nbq, c, (unsigned int)r | cls << 8);
+                atomicAdd(&ctr[kCtrClass + cls], 1u);
+            }
         }
+    }
+}
+
+// Pass 5: the items, ordered by cost class, most tiles first (a counting
+// sort over the classes), so that the tile kernel's queue hands out the
+// longest items first and its CTAs finish together.  Order within a class
+// is arbitrary; the sums do not depend on it.
+__global__ void __launch_bounds__(256)
+dense_order_kernel(const uint4 *__restrict__ raw, unsigned int *__restrict__ ctr,
+                   uint4 *__restrict__ items)
+{
+    __shared__ unsigned int base[kItemClasses];
+    if (threadIdx.x < kItemClasses) {
+        unsigned int b = 0;
+        for (unsigned int c = kItemClasses - 1; c > threadIdx.x; --c) b += ctr[kCtrClass + c];
+        base[threadIdx.x] = b;
+    }
+    __syncthreads();
+    const unsigned int total = ctr[kCtrItems];
+    for (unsigned int w = blockIdx.x * blockDim.x + threadIdx.x; w < total;
+         w += gridDim.x * blockDim.x) {
+        const uint4 it = raw[w];
+        const unsigned int cls = (it.w >> 8) & (kItemClasses - 1u);
+        items[base[cls] + atomicAdd(&ctr[kCtrFill + cls], 1u)] = it;
     }
 }
 
@@ -697,7 +738,7 @@ __device__ __forceinline__ float box_gap2(float3 ilo, float3 ihi, float3 jlo, fl
 // staged bodies and for the 4-byte j-side sums alike.
 __device__ __forceinline__ int swz(int k) { return ((k & 3) << 5) | (k >> 2); }
 
-// Grid-stride over the items.  For an item the CTA holds up to 128 bodies
+// Items come from a queue, longest first.  For an item the CTA holds up to 128 bodies
 // of the bucket b (one per thread, all in one cell), stages the neighbour
 // bucket nb in shared memory 128 bodies at a time, and each thread
 // collects the tile slots within r2 < 1 of its body before evaluating the
@@ -712,7 +753,7 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
                     const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
                     const unsigned int *__restrict__ state, long long *__restrict__ delta,
                     const __grid_constant__ LaunchTable tab, const uint4 *__restrict__ items,
-                    const unsigned int *__restrict__ nitems)
+                    unsigned int *__restrict__ ctr)
 {
     constexpr int kStride = 132;  // bytes per hit list row: rows start in distinct banks
     __shared__ float4 sp[128];    // x, y, z, body index (bits); NaN xyz outside the run
@@ -720,7 +761,8 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
     __shared__ float3 blo[4], bhi[4];  // box of each staged block of 32
     __shared__ unsigned int js[6][128];  // j-side sums of the staged slots (pair items)
     __shared__ unsigned char hits[128 * kStride];
-    const unsigned int total = *nitems;
+    __shared__ unsigned int s_item;
+    const unsigned int total = ctr[kCtrItems];
     const int t = threadIdx.x;
     const int tz = swz(t);  // where this thread stages its slot
     const int lane = t & 31, warp = t >> 5;
@@ -728,13 +770,18 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
     unsigned char *my = hits + t * kStride;
 #pragma unroll
     for (int d = 0; d < 6; ++d) js[d][t] = 0u;
-    for (unsigned int w = blockIdx.x; w < total; w += gridDim.x) {
+    for (;;) {
+        __syncthreads();  // every thread has read s_item and finished the last item
+        if (t == 0) s_item = atomicAdd(&ctr[kCtrHead], 1u);
+        __syncthreads();
+        const unsigned int w = s_item;
+        if (w >= total) break;
         const uint4 it = items[w];
         const unsigned int b = it.x, nb = it.y, chunk = it.z;
         const unsigned int bbeg = b ? cursor[b - 1] : 0u, bend = cursor[b];
         const unsigned int s0 = bbeg + 128u * chunk;
         const bool valid = s0 + (unsigned int)t < bend;
-        const RunDev &R = tab.runs[it.w];
+        const RunDev &R = tab.runs[it.w & 0xffu];
         const int rbeg = R.offset, rend = R.offset + R.n, sw = R.offset + R.nfe;
         const float inv_unit = tab.params[R.param].inv_unit;
         const unsigned int nbeg = nb ? cursor[nb - 1] : 0u, nend = cursor[nb];
@@ -847,13 +894,13 @@ static size_t dense_bucket_capacity(long long bodies)
 
 // Slot-ordered positions and velocities (float4, 8 words per slot); keys
 // (indexed by global body index) and sorted (by slot): max_end words each;
-// cursor and bucket state: one word per bucket each; block sums: 8192; item and
-// tiled-bucket counts (2 words) and up to 3 words to align the items to 16
-// bytes; items (4 words each); tiled buckets.
+// cursor and bucket state: one word per bucket each; block sums: 8192; the
+// tiled path's counters and up to 3 words to align the items to 16 bytes;
+// items as listed and as ordered (4 words each); tiled buckets.
 size_t gi_grid_words(long long max_end, long long bodies)
 {
     return 8 * (size_t)bodies + 2 * (size_t)max_end + 2 * (size_t)gi_grid_buckets(bodies) + 8192 +
-           2 + 3 + 4 * dense_item_capacity(bodies) + dense_bucket_capacity(bodies);
+           gi::kCtrWords + 3 + 8 * dense_item_capacity(bodies) + dense_bucket_capacity(bodies);
 }
 
 cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, cudaStream_t s)
@@ -881,11 +928,13 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     unsigned int *cursor = keys + 2 * (size_t)max_end;
     unsigned int *state = cursor + m;
     unsigned int *sums = state + m;
-    unsigned int *nitems = sums + 8192;
-    unsigned int *ntiled = nitems + 1;
-    uint4 *items = reinterpret_cast<uint4 *>((reinterpret_cast<uintptr_t>(nitems + 2) + 15) &
-                                             ~static_cast<uintptr_t>(15));
-    unsigned int *tiled = reinterpret_cast<unsigned int *>(items + dense_item_capacity(bodies));
+    unsigned int *ctr = sums + 8192;
+    unsigned int *ntiled = ctr + gi::kCtrTiled;
+    uint4 *raw = reinterpret_cast<uint4 *>((reinterpret_cast<uintptr_t>(ctr + gi::kCtrWords) + 15) &
+                                           ~static_cast<uintptr_t>(15));
+    const size_t icap = dense_item_capacity(bodies);
+    uint4 *items = raw + icap;
+    unsigned int *tiled = reinterpret_cast<unsigned int *>(items + icap);
     int maxn = 0;
     for (int r = 0; r < tab.nruns; ++r) maxn = std::max(maxn, tab.runs[r].n);
     if (maxn == 0) return cudaSuccess;
@@ -893,7 +942,7 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(state, 0, (size_t)m * sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(nitems, 0, 2 * sizeof(unsigned int), s);
+    e = cudaMemsetAsync(ctr, 0, gi::kCtrWords * sizeof(unsigned int), s);
     if (e != cudaSuccess) return e;
     const dim3 gk(std::min(4 * nsm, (maxn + 255) / 256), tab.nruns);
     gi::grid_keys<<<gk, 256, 0, s>>>(pos, tab, m - 1, keys, cursor);
@@ -908,12 +957,14 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
         cursor, m, dmin, state, tiled, ntiled);
     gi::dense_sort_kernel<<<2 * nsm, 256, 0, s>>>(pos, vel, cursor, sorted, spos, svel, tiled, ntiled);
     const int gt = (int)std::min<size_t>((dense_bucket_capacity(bodies) + 7) / 8, 4 * (size_t)nsm);
-    gi::dense_items_kernel<<<gt, 256, 0, s>>>(pos, tab, cursor, sorted, m - 1, state, tiled, ntiled,
-                                              items, nitems);
+    gi::dense_items_kernel<<<gt, 256, 0, s>>>(pos, tab, cursor, sorted, m - 1, state, tiled, ctr,
+                                              raw);
+    const int go = (int)std::min<size_t>((icap + 255) / 256, 4 * (size_t)nsm);
+    gi::dense_order_kernel<<<go, 256, 0, s>>>(raw, ctr, items);
     const dim3 gc((maxn + 7) / 8, tab.nruns);
     gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, spos, svel, cursor, sorted, keys, state, m - 1,
                                           delta, tab);
     gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(spos, svel, cursor, sorted, state, delta, tab,
-                                                     items, nitems);
+                                                     items, ctr);
     return cudaGetLastError();
 }
