@@ -526,11 +526,17 @@ __device__ __forceinline__ int run_of_body(const LaunchTable &tab, int i)
     return 0;
 }
 
-// Work item of the tiled path: x = bucket, y = neighbour bucket, z = chunk
-// of 128 of the bucket's bodies, w = run | cost class << 8.  Carrying all of
-// it saves the tile kernel a chain of dependent loads per item.  The cost
-// class is the number of 128-body tiles the item stages, minus one, capped
-// at kItemClasses - 1.
+// Work item of the tiled path, self-contained so that the tile kernel reads
+// it in one load, with no hop through the bucket bounds:
+//   x = first slot of the chunk of (up to) 128 bodies of bucket b,
+//   y = first slot of the neighbour bucket nb to stage (the chunk's own
+//       first slot when nb == b, else the start of nb),
+//   z = end of nb,
+//   w = run | cost class << 8 | pair << 12 | self << 13 | bodies of the
+//       chunk << 16.
+// The cost class is the number of 128-body tiles the item stages, minus
+// one, capped at kItemClasses - 1; pair: nb is tiled too (each pair is
+// evaluated once for both bodies); self: nb == b.
 constexpr unsigned int kItemClasses = 16;
 
 // Counters of the tiled path, in one block cleared per pass: item count,
@@ -599,10 +605,14 @@ dense_items_kernel(const float4 *__restrict__ pos, const __grid_constant__ Launc
             const unsigned int rank = __popc(km & ((1u << lane) - 1u));
             const unsigned int bbeg = b ? cursor[b - 1] : 0u;
             const unsigned int nbeg = nbq ? cursor[nbq - 1] : 0u, nend = cursor[nbq];
+            const unsigned int flags = (unsigned int)r | ((state[nbq] & kTiled) ? 1u << 12 : 0u) |
+                                       (nbq == b ? 1u << 13 : 0u);
             for (unsigned int c = 0; c < nch; ++c) {
-                const unsigned int first = nbq == b ? bbeg + 128u * c : nbeg;
+                const unsigned int s0 = bbeg + 128u * c;
+                const unsigned int first = nbq == b ? s0 : nbeg;
                 const unsigned int cls = min((nend - first + 127u) / 128u, kItemClasses) - 1u;
-                items[at + c * nq + rank] = make_uint4(b, nbq, c, (unsigned int)r | cls << 8);
+                const unsigned int ni = min(128u, bbeg + cnt - s0);
+                items[at + c * nq + rank] = make_uint4(s0, first, nend, flags | cls << 8 | ni << 16);
                 atomicAdd(&ctr[kCtrClass + cls], 1u);
             }
         }
@@ -761,7 +771,8 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
     __shared__ float3 blo[4], bhi[4];  // box of each staged block of 32
     __shared__ unsigned int js[6][128];  // j-side sums of the staged slots (pair items)
     __shared__ unsigned char hits[128 * kStride];
-    __shared__ unsigned int s_item;
+    __shared__ unsigned int s_w;  // the item to take next, and its record
+    __shared__ uint4 s_rec;
     const unsigned int total = ctr[kCtrItems];
     const int t = threadIdx.x;
     const int tz = swz(t);  // where this thread stages its slot
@@ -770,23 +781,30 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
     unsigned char *my = hits + t * kStride;
 #pragma unroll
     for (int d = 0; d < 6; ++d) js[d][t] = 0u;
+    // Thread 0 keeps the queue two items ahead: while the CTA works on one
+    // item, the record of the next is in flight and the one after is
+    // popped, so no item waits on the queue or on its record.
+    unsigned int w2 = 0u;  // thread 0: the item after next
+    if (t == 0) {
+        const unsigned int w1 = atomicAdd(&ctr[kCtrHead], 1u);
+        w2 = atomicAdd(&ctr[kCtrHead], 1u);
+        s_w = w1;
+        s_rec = w1 < total ? items[w1] : make_uint4(0u, 0u, 0u, 0u);
+    }
+    __syncthreads();
     for (;;) {
-        __syncthreads();  // every thread has read s_item and finished the last item
-        if (t == 0) s_item = atomicAdd(&ctr[kCtrHead], 1u);
-        __syncthreads();
-        const unsigned int w = s_item;
+        const unsigned int w = s_w;
         if (w >= total) break;
-        const uint4 it = items[w];
-        const unsigned int b = it.x, nb = it.y, chunk = it.z;
-        const unsigned int bbeg = b ? cursor[b - 1] : 0u, bend = cursor[b];
-        const unsigned int s0 = bbeg + 128u * chunk;
-        const bool valid = s0 + (unsigned int)t < bend;
-        const RunDev &R = tab.runs[it.w & 0xffu];
+        const uint4 rec = s_rec;
+        unsigned int nw = 0u;  // thread 0: the next item and its record
+        uint4 nrec = make_uint4(0u, 0u, 0u, 0u);
+        const unsigned int s0 = rec.x, first = rec.y, nend = rec.z;
+        const unsigned int ni = rec.w >> 16;
+        const bool pair = (rec.w >> 12) & 1u, self = (rec.w >> 13) & 1u;
+        const bool valid = (unsigned int)t < ni;
+        const RunDev &R = tab.runs[rec.w & 0xffu];
         const int rbeg = R.offset, rend = R.offset + R.n, sw = R.offset + R.nfe;
         const float inv_unit = tab.params[R.param].inv_unit;
-        const unsigned int nbeg = nb ? cursor[nb - 1] : 0u, nend = cursor[nb];
-        const bool pair = (state[nb] & kTiled) != 0u;
-        const unsigned int first = nb == b ? s0 : nbeg;
         const int i = valid ? sorted[s0 + t] : -1;
         const float4 pi = valid ? spos[s0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 vi = valid ? svel[s0 + t] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -800,6 +818,11 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
         for (unsigned int base = first; base < nend; base += 128u) {
             __syncthreads();  // the previous tile is consumed
             if (pair && base != first) flush_slot(js, tz, __float_as_int(sp[tz].w), delta);
+            if (t == 0 && base == first) {  // every thread has read s_w and s_rec
+                nw = w2;
+                nrec = w2 < total ? items[w2] : make_uint4(0u, 0u, 0u, 0u);
+                w2 = atomicAdd(&ctr[kCtrHead], 1u);
+            }
             const unsigned int u = base + (unsigned int)t;
             float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
             if (u < nend) {
@@ -822,7 +845,7 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
             __syncthreads();
             if (!valid) continue;
             const int cnt = (int)min(128u, nend - base);
-            const int kmin = (nb == b && base == s0) ? t + 1 : 0;  // own tile: each pair once
+            const int kmin = (self && base == first) ? t + 1 : 0;  // own tile: each pair once
             int nh = 0;
             for (int s = 0; s < 4 && 32 * s < cnt; ++s) {
                 if (box_gap2(ilo, ihi, blo[s], bhi[s]) >= 1.0f) continue;  // the same for the warp
@@ -855,8 +878,13 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
                 else fix_add3(acc, c, dx, dy, dz);
             }
         }
-        __syncthreads();  // the last tile's j-side sums are complete
-        if (pair && first < nend) flush_slot(js, tz, __float_as_int(sp[tz].w), delta);
+        __syncthreads();  // the last tile's j-side sums are complete; s_w, s_rec are read
+        if (pair) flush_slot(js, tz, __float_as_int(sp[tz].w), delta);
+        if (t == 0) {
+            s_w = nw;
+            s_rec = nrec;
+        }
+        __syncthreads();  // the next item's index and record are visible
         fix_fold(acc);
         const long long ax = acc.x, ay = acc.y, az = acc.z;
         if (valid && (ax | ay | az)) {
