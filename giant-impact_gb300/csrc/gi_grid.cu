@@ -771,8 +771,7 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
     __shared__ float3 blo[4], bhi[4];  // box of each staged block of 32
     __shared__ unsigned int js[6][128];  // j-side sums of the staged slots (pair items)
     __shared__ unsigned char hits[128 * kStride];
-    __shared__ unsigned int s_w;  // the item to take next, and its record
-    __shared__ uint4 s_rec;
+    __shared__ unsigned int s_w;  // the item to take next
     const unsigned int total = ctr[kCtrItems];
     const int t = threadIdx.x;
     const int tz = swz(t);  // where this thread stages its slot
@@ -781,23 +780,16 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
     unsigned char *my = hits + t * kStride;
 #pragma unroll
     for (int d = 0; d < 6; ++d) js[d][t] = 0u;
-    // Thread 0 keeps the queue two items ahead: while the CTA works on one
-    // item, the record of the next is in flight and the one after is
-    // popped, so no item waits on the queue or on its record.
-    unsigned int w2 = 0u;  // thread 0: the item after next
-    if (t == 0) {
-        const unsigned int w1 = atomicAdd(&ctr[kCtrHead], 1u);
-        w2 = atomicAdd(&ctr[kCtrHead], 1u);
-        s_w = w1;
-        s_rec = w1 < total ? items[w1] : make_uint4(0u, 0u, 0u, 0u);
-    }
+    // Thread 0 takes the next item from the queue when the current one
+    // reaches its last tile: the atomic's latency hides behind that tile,
+    // and the CTA still takes items close to the queue's longest-first order.
+    if (t == 0) s_w = atomicAdd(&ctr[kCtrHead], 1u);
     __syncthreads();
     for (;;) {
         const unsigned int w = s_w;
         if (w >= total) break;
-        const uint4 rec = s_rec;
-        unsigned int nw = 0u;  // thread 0: the next item and its record
-        uint4 nrec = make_uint4(0u, 0u, 0u, 0u);
+        const uint4 rec = items[w];
+        unsigned int nw = 0u;  // thread 0: the next item
         const unsigned int s0 = rec.x, first = rec.y, nend = rec.z;
         const unsigned int ni = rec.w >> 16;
         const bool pair = (rec.w >> 12) & 1u, self = (rec.w >> 13) & 1u;
@@ -818,11 +810,7 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
         for (unsigned int base = first; base < nend; base += 128u) {
             __syncthreads();  // the previous tile is consumed
             if (pair && base != first) flush_slot(js, tz, __float_as_int(sp[tz].w), delta);
-            if (t == 0 && base == first) {  // every thread has read s_w and s_rec
-                nw = w2;
-                nrec = w2 < total ? items[w2] : make_uint4(0u, 0u, 0u, 0u);
-                w2 = atomicAdd(&ctr[kCtrHead], 1u);
-            }
+            if (t == 0 && base + 128u >= nend) nw = atomicAdd(&ctr[kCtrHead], 1u);
             const unsigned int u = base + (unsigned int)t;
             float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
             if (u < nend) {
@@ -878,13 +866,10 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
                 else fix_add3(acc, c, dx, dy, dz);
             }
         }
-        __syncthreads();  // the last tile's j-side sums are complete; s_w, s_rec are read
+        __syncthreads();  // the last tile's j-side sums are complete; s_w is read
         if (pair) flush_slot(js, tz, __float_as_int(sp[tz].w), delta);
-        if (t == 0) {
-            s_w = nw;
-            s_rec = nrec;
-        }
-        __syncthreads();  // the next item's index and record are visible
+        if (t == 0) s_w = nw;
+        __syncthreads();  // the next item's index is visible
         fix_fold(acc);
         const long long ax = acc.x, ay = acc.y, az = acc.z;
         if (valid && (ax | ay | az)) {
