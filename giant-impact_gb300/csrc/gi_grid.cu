@@ -22,10 +22,11 @@
 // The all-pairs epilogue adds the correction before its single rounding.
 //
 // Two passes share the bodies.  contact_kernel gives one warp to each body
-// of an ordinary cell.  Dense buckets (at least gi_options.dense_min bodies,
-// 256 by default, e.g. an interpenetrating collision remnant with thousands
-// of contacts per body) whose bodies all share one cell are sorted by
-// sub-cell and go through contact_tile_kernel: a work item is (bucket,
+// of an ordinary cell.  Crowded buckets (gi_options.dense_min bodies, 256 by
+// default, or a quarter of that next to such a cell; e.g. an
+// interpenetrating collision remnant with thousands of contacts per body)
+// whose bodies all share one cell are sorted by sub-cell and go through
+// contact_tile_kernel: a work item is (bucket,
 // neighbour bucket, chunk of 128 of its bodies); its CTA stages the
 // neighbour bucket in shared memory 128 bodies at a time, each thread
 // filters the tile into a hit list and evaluates the law on the hits only,
@@ -334,12 +335,26 @@ __device__ __forceinline__ void flush_slot(unsigned int (*js)[128], int t, int j
     }
 }
 
-// Buckets of at least tab.dense_min bodies (256 unless set) whose bodies
-// share one cell take the tiled path; at least kDenseFloor, which bounds
-// the item count.  Bucket state bits: 1 = mixed cells (stays on the warp
-// path), 2 = tiled.
+// A bucket whose bodies share one cell takes the tiled path when it holds
+// at least tab.dense_min bodies (256 unless set), or at least a quarter of
+// that next to a cell that does: near a crowded remnant its bodies have
+// enough contacts to pay the tiled path's fixed costs per item, while the
+// cores of settled bodies (cells of tens to a few hundred bodies, ~20
+// contacts a body) stay on the warp path.  Either bound is at least
+// kDenseFloor, which bounds the item count.  Bucket state bits: 1 = mixed
+// cells (stays on the warp path), 2 = tiled.
 constexpr unsigned int kDenseFloor = 32;
 constexpr unsigned int kMixed = 1u, kTiled = 2u;
+
+__host__ __device__ __forceinline__ unsigned int dense_hi(unsigned int dmin)
+{
+    return dmin > kDenseFloor ? dmin : kDenseFloor;
+}
+
+__host__ __device__ __forceinline__ unsigned int dense_lo(unsigned int dmin)
+{
+    return dmin / 4u > kDenseFloor ? dmin / 4u : kDenseFloor;
+}
 
 // Contact correction of body i (run r) by one warp.  Lanes 0..26 look up
 // the 27 neighbour buckets at once (one memory round trip; a bucket that
@@ -488,10 +503,10 @@ contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                       tab.sep_test, blockIdx.y, i, lane, hitq[threadIdx.x >> 5]);
 }
 
-// Pass 1, one thread per body of the run blockIdx.y: for bodies of dense
-// buckets, clear the correction (the tiled path adds into it) and mark the
-// bucket mixed when the body's cell or run differs from the bucket's first
-// body.
+// Pass 1, one thread per body of the run blockIdx.y: for bodies of buckets
+// that may be tiled (at least dense_lo bodies), clear the correction (the
+// tiled path adds into it; the warp path overwrites it) and mark the bucket
+// mixed when the body's cell or run differs from the bucket's first body.
 __global__ void __launch_bounds__(256)
 dense_check_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
                    const unsigned int *__restrict__ keys, const unsigned int *__restrict__ cursor,
@@ -499,11 +514,11 @@ dense_check_kernel(const float4 *__restrict__ pos, const __grid_constant__ Launc
                    long long *__restrict__ delta)
 {
     const RunDev &R = tab.runs[blockIdx.y];
-    dmin = max(dmin, kDenseFloor);
+    const unsigned int lo = dense_lo(dmin);
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < R.n; k += gridDim.x * blockDim.x) {
         const int i = R.offset + k;
         const unsigned int b = keys[i];
-        if (bucket_size(cursor, b) < dmin) continue;
+        if (bucket_size(cursor, b) < lo) continue;
         delta[3 * (size_t)i + 0] = 0;
         delta[3 * (size_t)i + 1] = 0;
         delta[3 * (size_t)i + 2] = 0;
@@ -545,16 +560,29 @@ constexpr unsigned int kItemClasses = 16;
 constexpr int kCtrItems = 0, kCtrTiled = 1, kCtrHead = 2, kCtrClass = 4,
               kCtrFill = 4 + (int)kItemClasses, kCtrWords = 4 + 2 * (int)kItemClasses;
 
-// Pass 2, one thread per bucket: a dense bucket of one cell becomes tiled
-// and is listed in tiled[0 .. *ntiled).
+// Pass 2, one thread per bucket: a crowded bucket of one cell (see
+// dense_hi, dense_lo) becomes tiled and is listed in tiled[0 .. *ntiled).
 __global__ void __launch_bounds__(256)
-dense_mark_kernel(const unsigned int *__restrict__ cursor, unsigned int m, unsigned int dmin,
-                  unsigned int *state, unsigned int *__restrict__ tiled,
-                  unsigned int *__restrict__ ntiled)
+dense_mark_kernel(const float4 *__restrict__ pos, const __grid_constant__ LaunchTable tab,
+                  const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
+                  unsigned int m, unsigned int mask, unsigned int dmin, unsigned int *state,
+                  unsigned int *__restrict__ tiled, unsigned int *__restrict__ ntiled)
 {
-    dmin = max(dmin, kDenseFloor);
+    const unsigned int hi = dense_hi(dmin), lo = dense_lo(dmin);
     for (unsigned int b = blockIdx.x * blockDim.x + threadIdx.x; b < m; b += gridDim.x * blockDim.x) {
-        if (bucket_size(cursor, b) < dmin || (state[b] & kMixed)) continue;
+        const unsigned int n = bucket_size(cursor, b);
+        if (n < lo || (state[b] & kMixed)) continue;
+        bool crowded = n >= hi;
+        if (!crowded) {  // a neighbour cell of at least hi bodies?
+            const int j0 = sorted[b ? cursor[b - 1] : 0u];
+            const int r = run_of_body(tab, j0);
+            const float4 p = pos[j0];
+            const int cx = cell_of(p.x), cy = cell_of(p.y), cz = cell_of(p.z);
+            for (int q = 0; q < 27 && !crowded; ++q)
+                crowded = bucket_size(cursor, bucket_of(r, cx + q % 3 - 1, cy + (q / 3) % 3 - 1,
+                                                        cz + q / 9 - 1, mask)) >= hi;
+        }
+        if (!crowded) continue;
         state[b] = kTiled;
         tiled[atomicAdd(ntiled, 1u)] = b;
     }
@@ -967,7 +995,7 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     const unsigned int dmin = (unsigned int)tab.dense_min;
     gi::dense_check_kernel<<<gk, 256, 0, s>>>(pos, tab, keys, cursor, sorted, dmin, state, delta);
     gi::dense_mark_kernel<<<std::min((int)((m + 255) / 256), 4 * nsm), 256, 0, s>>>(
-        cursor, m, dmin, state, tiled, ntiled);
+        pos, tab, cursor, sorted, m, m - 1, dmin, state, tiled, ntiled);
     gi::dense_sort_kernel<<<2 * nsm, 256, 0, s>>>(pos, vel, cursor, sorted, spos, svel, tiled, ntiled);
     const int gt = (int)std::min<size_t>((dense_bucket_capacity(bodies) + 7) / 8, 4 * (size_t)nsm);
     gi::dense_items_kernel<<<gt, 256, 0, s>>>(pos, tab, cursor, sorted, m - 1, state, tiled, ctr,
