@@ -156,8 +156,9 @@ typedef struct gi_run {
 typedef struct gi_options {
     int sep_test;          /* GI_SEP_*, default GI_SEP_REF_INT */
     int accum;             /* GI_ACCUM_*, default GI_ACCUM_KAHAN */
-    int dense_min;         /* contact pass: cells of at least this many bodies
-                              take the shared-memory tiled path; 0 = 256.
+    int dense_min;         /* contact pass: cells of at least this many bodies,
+                              or of a quarter of it next to such a cell, take
+                              the shared-memory tiled path; 0 = 256.
                               Results do not depend on it. */
 } gi_options;
 
