@@ -166,7 +166,7 @@ __device__ __forceinline__ void process_item(const int item, const ForceArgs &a,
             for (int k = 0; k < IPT; ++k)
                 tx[k] = ty[k] = tz[k] = make_float2(0.0f, 0.0f);
 
-#pragma unroll(IPT >= 8 ? 2 : (IPT >= 4 ? 4 : 16))
+#pragma unroll(IPT >= 8 ? 2 : (IPT >= 4 ? 4 : 32))
             for (int jp = 0; jp < GI_NT / 2; ++jp) {
                 const float4 qa = sm.A[jp];
                 const float2 qz = sm.B[jp];
