@@ -1222,7 +1222,7 @@ long long gi_internal_scratch_bytes(gi_ctx *c, int n)
     tuning_for(c, n, &ipt, &jc);
     chunking(n, jc, &lg, &tiles, &nsplit);
     const long long partials = nsplit > 1 ? (long long)nsplit * 3 * 8 * n : 0;
-    const long long contacts = 24LL * n + 8LL * n + 4LL * gi_grid_buckets(n) + 4LL * 8192;
+    const long long contacts = 24LL * n + 4LL * (long long)gi_grid_words(n, n);  // delta + grid
     const long long tickets = 4LL * ((n + GI_NT - 1) / GI_NT);
     return partials + contacts + tickets;
 }
