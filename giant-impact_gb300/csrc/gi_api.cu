@@ -248,6 +248,11 @@ struct StreamScratch {
     size_t grid_work_cap = 0;           // words
     long long *delta = nullptr;         // contact corrections, 3 per body
     size_t delta_cap = 0;               // bodies
+    double *fsum = nullptr;             // far-field sums of GI_EPI_SUM launches, 3 per body
+    // The contact pass runs on `aux`, beside the far field on the caller's
+    // stream: forked after the previous step, joined before the epilogue.
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 struct gi_ctx {
@@ -285,8 +290,9 @@ static int ctx_init(gi_ctx *c, int device)
     DeviceGuard g(device);
     for (int acc = 0; acc < 3; ++acc)
         for (int p : {1, 2, 4, 8}) {
-            const int o = std::min(gi_force_occupancy(p, acc, GI_EPI_FORCE),
-                                   gi_force_occupancy(p, acc, GI_EPI_STEP));
+            const int o = std::min({gi_force_occupancy(p, acc, GI_EPI_FORCE),
+                                    gi_force_occupancy(p, acc, GI_EPI_STEP),
+                                    gi_force_occupancy(p, acc, GI_EPI_SUM)});
             c->occ[acc][p] = std::max(o, 1);
         }
     return GI_OK;
@@ -304,6 +310,10 @@ static void ctx_free(gi_ctx *c)
         cudaFree(x.pp_vel);
         cudaFree(x.grid_work);
         cudaFree(x.delta);
+        cudaFree(x.fsum);
+        if (x.ev_fork) cudaEventDestroy(x.ev_fork);
+        if (x.ev_join) cudaEventDestroy(x.ev_join);
+        if (x.aux) cudaStreamDestroy(x.aux);
     }
     c->scratch.clear();
     cudaFree(c->mirror_pos);
@@ -554,7 +564,7 @@ static int ensure_scratch(gi_ctx *c, const Plan &plan, cudaStream_t s, StreamScr
     for (long long b : plan.bodies) gwords = std::max(gwords, gi_grid_words(plan.max_end, b));
     const bool grow_g = gwords > x.grid_work_cap;
     const bool grow_d = (size_t)plan.max_end > x.delta_cap;
-    if (!grow_t && !grow_p && !grow_g && !grow_d && x.queue) return GI_OK;
+    if (!grow_t && !grow_p && !grow_g && !grow_d && x.queue && x.aux) return GI_OK;
     if (stream_capturing(s))
         return fail(GI_ERR_INVALID_ARG,
                     "scratch must grow (run once outside stream capture before capturing)");
@@ -562,6 +572,14 @@ static int ensure_scratch(gi_ctx *c, const Plan &plan, cudaStream_t s, StreamScr
     if (!x.queue) {
         GI_CUDA(cudaMalloc(&x.queue, 2 * sizeof(unsigned int)), "cudaMalloc queue");
         GI_CUDA(cudaMemset(x.queue, 0, 2 * sizeof(unsigned int)), "cudaMemset queue");
+    }
+    if (!x.aux) {
+        int lo = 0, hi = 0;  // hi: the greatest priority (numerically lowest)
+        GI_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi), "cudaDeviceGetStreamPriorityRange");
+        GI_CUDA(cudaStreamCreateWithPriority(&x.aux, cudaStreamNonBlocking, hi),
+                "cudaStreamCreateWithPriority");
+        GI_CUDA(cudaEventCreateWithFlags(&x.ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+        GI_CUDA(cudaEventCreateWithFlags(&x.ev_join, cudaEventDisableTiming), "cudaEventCreate");
     }
     if (grow_t) {
         cudaFree(x.tickets);
@@ -589,9 +607,12 @@ static int ensure_scratch(gi_ctx *c, const Plan &plan, cudaStream_t s, StreamScr
     }
     if (grow_d) {
         cudaFree(x.delta);
+        cudaFree(x.fsum);
         x.delta = nullptr;
+        x.fsum = nullptr;
         x.delta_cap = 0;
         GI_CUDA(cudaMalloc(&x.delta, (size_t)plan.max_end * 3 * sizeof(long long)), "cudaMalloc delta");
+        GI_CUDA(cudaMalloc(&x.fsum, (size_t)plan.max_end * 3 * sizeof(double)), "cudaMalloc fsum");
         x.delta_cap = plan.max_end;
     }
     return GI_OK;
@@ -610,11 +631,19 @@ static int convert_params(const gi_pair_params *params, int nparams, std::vector
     return GI_OK;
 }
 
+// One force evaluation (or fused step) per table.  The contact pass and the
+// far field are independent until the epilogue, so they run side by side:
+// the contact pass on the scratch's aux stream, forked from the caller's
+// stream; the far field on the caller's stream with half its resident CTAs
+// per SM (FMA-bound, it runs as fast at half occupancy and leaves room on
+// every SM for the contact kernels); then, joined, the epilogue, which adds
+// the corrections with the fused epilogue's arithmetic.
 static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, int epi,
                           const float4 *pos, const float4 *vel, float4 *force,
                           float4 *pos_out, float4 *vel_out, cudaStream_t s)
 {
     for (size_t t = 0; t < plan.tables.size(); ++t) {
+        const LaunchTable &tab = plan.tables[t];
         ForceArgs a;
         a.pos = pos;
         a.vel = vel;
@@ -625,14 +654,21 @@ static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, i
         a.tickets = x->tickets;
         a.queue = x->queue;
         a.delta = x->delta;
-        // contact pass first: the force epilogue adds its corrections
-        GI_CUDA(gi_launch_contacts(pos, vel, plan.tables[t], plan.bodies[t], plan.max_end,
-                                   x->grid_work, x->delta, c->sm_count, s),
+        a.fsum = x->fsum;
+        GI_CUDA(cudaEventRecord(x->ev_fork, s), "cudaEventRecord");
+        GI_CUDA(cudaStreamWaitEvent(x->aux, x->ev_fork, 0), "cudaStreamWaitEvent");
+        GI_CUDA(gi_launch_contacts(pos, vel, tab, plan.bodies[t], plan.max_end, x->grid_work,
+                                   x->delta, c->sm_count, x->aux),
                 "contact pass");
+        GI_CUDA(cudaEventRecord(x->ev_join, x->aux), "cudaEventRecord");
         const int p = plan.ipt[t];
-        const int grid = c->sm_count * c->occ[c->opt.accum][p];
-        GI_CUDA(gi_launch_force(p, c->opt.accum, epi, a, plan.tables[t], grid, s),
+        const int grid = c->sm_count * std::max(1, (c->occ[c->opt.accum][p] + 1) / 2);
+        GI_CUDA(gi_launch_force(p, c->opt.accum, GI_EPI_SUM, a, tab, grid, s),
                 "force kernel launch");
+        GI_CUDA(cudaStreamWaitEvent(s, x->ev_join, 0), "cudaStreamWaitEvent");
+        int maxn = 0;
+        for (int r = 0; r < tab.nruns; ++r) maxn = std::max(maxn, tab.runs[r].n);
+        GI_CUDA(gi_launch_finish(epi, a, tab, maxn, c->sm_count, s), "epilogue launch");
     }
     return GI_OK;
 }

@@ -79,6 +79,38 @@ __device__ __forceinline__ float contact_mag(float G, float K, float r2)
     return __fmaf_rn(-K, dlo, __fmaf_rn(-K, dhi, G));
 }
 
+// F = far-field sum + contact correction, rounded once to float; stored as
+// the force (GI_EPI_FORCE) or applied as the kick-drift into the other
+// state buffer (GI_EPI_STEP).  Shared by the fused epilogue and
+// finish_kernel, so both give the same bits.
+template <int EPI>
+__device__ __forceinline__ void finish_body(const ForceArgs &a, const RunDev &R, double unit,
+                                            int i, const double fd[3])
+{
+    const long long *dl = a.delta + 3 * (size_t)i;
+    const float fx = (float)(fd[0] + (double)__ldcg(dl + 0) * unit);
+    const float fy = (float)(fd[1] + (double)__ldcg(dl + 1) * unit);
+    const float fz = (float)(fd[2] + (double)__ldcg(dl + 2) * unit);
+    if (EPI == GI_EPI_FORCE) {
+        float *f = reinterpret_cast<float *>(a.force + i);
+        f[0] = fx; f[1] = fy; f[2] = fz;
+    } else {
+        // v += (F - damp v) dt/m ; x += v dt  (impactAddTime.cu:384-393,
+        // generateTargetImpactor.cu:636-663), .w carried through.
+        const float dtm = (i < R.offset + R.nfe) ? R.dtm_fe : R.dtm_si;
+        float4 v = __ldg(&a.vel[i]);
+        float4 p = __ldg(&a.pos[i]);
+        v.x = __fmaf_rn(__fmaf_rn(-R.damp, v.x, fx), dtm, v.x);
+        v.y = __fmaf_rn(__fmaf_rn(-R.damp, v.y, fy), dtm, v.y);
+        v.z = __fmaf_rn(__fmaf_rn(-R.damp, v.z, fz), dtm, v.z);
+        p.x = __fmaf_rn(v.x, R.dt, p.x);
+        p.y = __fmaf_rn(v.y, R.dt, p.y);
+        p.z = __fmaf_rn(v.z, R.dt, p.z);
+        a.vel_out[i] = v;
+        a.pos_out[i] = p;
+    }
+}
+
 // Shared memory of one CTA: the staged j-tile and the running sums of its
 // GI_NT * IPT i-bodies.  The sums are touched once per tile (the fold), so
 // they live here rather than in registers.
@@ -281,27 +313,13 @@ __device__ __forceinline__ void process_item(const int item, const ForceArgs &a,
     for (int k = 0; k < IPT; ++k) {
         const int i = i0 + k * GI_NT + tid;
         if (i >= rend) continue;
-        const long long *dl = a.delta + 3 * (size_t)i;
-        const float fx = (float)(fd[k][0] + (double)__ldcg(dl + 0) * unit);
-        const float fy = (float)(fd[k][1] + (double)__ldcg(dl + 1) * unit);
-        const float fz = (float)(fd[k][2] + (double)__ldcg(dl + 2) * unit);
-        if (EPI == GI_EPI_FORCE) {
-            float *f = reinterpret_cast<float *>(a.force + i);
-            f[0] = fx; f[1] = fy; f[2] = fz;
+        if (EPI == GI_EPI_SUM) {  // finish_kernel adds the contacts once they are done
+            double *q = a.fsum + 3 * (size_t)i;
+            q[0] = fd[k][0];
+            q[1] = fd[k][1];
+            q[2] = fd[k][2];
         } else {
-            // v += (F - damp v) dt/m ; x += v dt  (impactAddTime.cu:384-393,
-            // generateTargetImpactor.cu:636-663), .w carried through.
-            const float dtm = (i < sw) ? R.dtm_fe : R.dtm_si;
-            float4 v = __ldg(&a.vel[i]);
-            float4 p = __ldg(&pos[i]);
-            v.x = __fmaf_rn(__fmaf_rn(-R.damp, v.x, fx), dtm, v.x);
-            v.y = __fmaf_rn(__fmaf_rn(-R.damp, v.y, fy), dtm, v.y);
-            v.z = __fmaf_rn(__fmaf_rn(-R.damp, v.z, fz), dtm, v.z);
-            p.x = __fmaf_rn(v.x, R.dt, p.x);
-            p.y = __fmaf_rn(v.y, R.dt, p.y);
-            p.z = __fmaf_rn(v.z, R.dt, p.z);
-            a.vel_out[i] = v;
-            a.pos_out[i] = p;
+            finish_body<EPI>(a, R, unit, i, fd[k]);
         }
     }
 }
@@ -351,6 +369,9 @@ cudaError_t launch_force_ipt(int acc, int epi, const ForceArgs &a, const LaunchT
     GI_CASE(GI_ACC_FP32, GI_EPI_STEP)
     GI_CASE(GI_ACC_FP64, GI_EPI_FORCE)
     GI_CASE(GI_ACC_FP64, GI_EPI_STEP)
+    GI_CASE(GI_ACC_KAHAN, GI_EPI_SUM)
+    GI_CASE(GI_ACC_FP32, GI_EPI_SUM)
+    GI_CASE(GI_ACC_FP64, GI_EPI_SUM)
 #undef GI_CASE
     return cudaErrorInvalidValue;
 }
@@ -369,8 +390,28 @@ int occupancy_ipt(int acc, int epi)
     GI_OCC(GI_ACC_FP32, GI_EPI_STEP)
     GI_OCC(GI_ACC_FP64, GI_EPI_FORCE)
     GI_OCC(GI_ACC_FP64, GI_EPI_STEP)
+    GI_OCC(GI_ACC_KAHAN, GI_EPI_SUM)
+    GI_OCC(GI_ACC_FP32, GI_EPI_SUM)
+    GI_OCC(GI_ACC_FP64, GI_EPI_SUM)
 #undef GI_OCC
     return e == cudaSuccess ? nb : 0;
+}
+
+// The far field's epilogue, split off (GI_EPI_SUM): one thread per body of
+// the run blockIdx.y adds the contact corrections to the FP64 sums in fsum
+// and stores the force or applies the kick-drift, as the fused epilogue does.
+template <int EPI>
+__global__ void __launch_bounds__(256) finish_kernel(const ForceArgs a,
+                                                     const __grid_constant__ LaunchTable tab)
+{
+    const RunDev &R = tab.runs[blockIdx.y];
+    const double unit = tab.params[R.param].fx_unit;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < R.n; k += gridDim.x * blockDim.x) {
+        const int i = R.offset + k;
+        const double *q = a.fsum + 3 * (size_t)i;
+        const double fd[3] = {__ldcg(q), __ldcg(q + 1), __ldcg(q + 2)};
+        finish_body<EPI>(a, R, unit, i, fd);
+    }
 }
 
 }  // namespace gi

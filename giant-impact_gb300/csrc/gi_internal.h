@@ -24,6 +24,7 @@
 
 #define GI_EPI_FORCE 0  // write force[i].xyz
 #define GI_EPI_STEP 1   // fused kick-drift into the other state buffer
+#define GI_EPI_SUM 2    // FP64 far-field sums into fsum; gi_launch_finish completes
 
 // Pair constants indexed by the pair class test = (i is Fe) + (j is Fe):
 // 0 = Si-Si, 1 = Fe-Si, 2 = Fe-Fe.
@@ -72,6 +73,7 @@ struct ForceArgs {
     unsigned int *tickets;
     unsigned int *queue;  // [0] next work item, [1] CTAs finished (zero between launches)
     const long long *delta;  // contact corrections, 3 per body, fixed point (gi_grid.cu)
+    double *fsum;            // GI_EPI_SUM: far-field sums, 3 per body
 };
 
 // Launchers (gi_force_ipt*.cu).  Return cudaError_t of the launch.
@@ -83,6 +85,10 @@ cudaError_t gi_launch_force_ipt4(int acc, int epi, const ForceArgs &a, const Lau
 cudaError_t gi_launch_force_ipt8(int acc, int epi, const ForceArgs &a, const LaunchTable &tab, int grid, cudaStream_t s);
 // Resident CTAs per SM of a force kernel instance (for the planner).
 int gi_force_occupancy(int ipt, int acc, int epi);
+// The epilogue of a GI_EPI_SUM launch (epi = GI_EPI_FORCE or GI_EPI_STEP):
+// adds the contact corrections and stores or steps, one thread per body.
+cudaError_t gi_launch_finish(int epi, const ForceArgs &a, const LaunchTable &tab, int maxn,
+                             int nsm, cudaStream_t s);
 
 // gi_grid.cu: contact corrections of every body of the table's runs into
 // delta (3 x int64 per body) through a hashed cell grid.

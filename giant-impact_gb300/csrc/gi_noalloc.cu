@@ -168,6 +168,7 @@ extern "C" int gi_forces_collision_noalloc(const float *pos, const float *vel, f
     a.tickets = tickets;
     a.queue = queue;
     a.delta = delta;
+    a.fsum = nullptr;  // fused epilogue (GI_EPI_FORCE)
     int occ = gi_force_occupancy(kIpt, GI_ACC_KAHAN, GI_EPI_FORCE);
     if (occ < 1) occ = 1;
     if (gi_launch_force(kIpt, GI_ACC_KAHAN, GI_EPI_FORCE, a, tab, nsm * occ, s) != cudaSuccess)
