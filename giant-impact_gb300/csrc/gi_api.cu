@@ -631,13 +631,20 @@ static int convert_params(const gi_pair_params *params, int nparams, std::vector
     return GI_OK;
 }
 
+// Tables of up to this many pairs (sum of n^2 over their runs) run the
+// contact pass beside the far field; larger ones, where the contact pass is
+// a sliver of the step and the far field wants every resident CTA, run it
+// first and take the fused epilogue.
+constexpr long long kOverlapMaxPairs = 1LL << 34;
+
 // One force evaluation (or fused step) per table.  The contact pass and the
-// far field are independent until the epilogue, so they run side by side:
-// the contact pass on the scratch's aux stream, forked from the caller's
-// stream; the far field on the caller's stream with half its resident CTAs
-// per SM (FMA-bound, it runs as fast at half occupancy and leaves room on
-// every SM for the contact kernels); then, joined, the epilogue, which adds
-// the corrections with the fused epilogue's arithmetic.
+// far field are independent until the epilogue, so for tables of up to
+// kOverlapMaxPairs pairs they run side by side: the contact pass on the
+// scratch's aux stream, forked from the caller's stream; the far field on
+// the caller's stream with half its resident CTAs per SM (at that size it
+// runs as fast at half occupancy and leaves room on every SM for the contact
+// kernels); then, joined, the epilogue, with the fused epilogue's
+// arithmetic.  Either way the results are the same bits.
 static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, int epi,
                           const float4 *pos, const float4 *vel, float4 *force,
                           float4 *pos_out, float4 *vel_out, cudaStream_t s)
@@ -655,19 +662,32 @@ static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, i
         a.queue = x->queue;
         a.delta = x->delta;
         a.fsum = x->fsum;
+        int maxn = 0;
+        long long pairs = 0;
+        for (int r = 0; r < tab.nruns; ++r) {
+            maxn = std::max(maxn, tab.runs[r].n);
+            pairs += (long long)tab.runs[r].n * tab.runs[r].n;
+        }
+        const int p = plan.ipt[t];
+        const int occ = c->occ[c->opt.accum][p];
+        if (pairs > kOverlapMaxPairs) {
+            GI_CUDA(gi_launch_contacts(pos, vel, tab, plan.bodies[t], plan.max_end, x->grid_work,
+                                       x->delta, c->sm_count, s),
+                    "contact pass");
+            GI_CUDA(gi_launch_force(p, c->opt.accum, epi, a, tab, c->sm_count * occ, s),
+                    "force kernel launch");
+            continue;
+        }
         GI_CUDA(cudaEventRecord(x->ev_fork, s), "cudaEventRecord");
         GI_CUDA(cudaStreamWaitEvent(x->aux, x->ev_fork, 0), "cudaStreamWaitEvent");
         GI_CUDA(gi_launch_contacts(pos, vel, tab, plan.bodies[t], plan.max_end, x->grid_work,
                                    x->delta, c->sm_count, x->aux),
                 "contact pass");
         GI_CUDA(cudaEventRecord(x->ev_join, x->aux), "cudaEventRecord");
-        const int p = plan.ipt[t];
-        const int grid = c->sm_count * std::max(1, (c->occ[c->opt.accum][p] + 1) / 2);
-        GI_CUDA(gi_launch_force(p, c->opt.accum, GI_EPI_SUM, a, tab, grid, s),
+        GI_CUDA(gi_launch_force(p, c->opt.accum, GI_EPI_SUM, a, tab,
+                                c->sm_count * std::max(1, (occ + 1) / 2), s),
                 "force kernel launch");
         GI_CUDA(cudaStreamWaitEvent(s, x->ev_join, 0), "cudaStreamWaitEvent");
-        int maxn = 0;
-        for (int r = 0; r < tab.nruns; ++r) maxn = std::max(maxn, tab.runs[r].n);
         GI_CUDA(gi_launch_finish(epi, a, tab, maxn, c->sm_count, s), "epilogue launch");
     }
     return GI_OK;
