@@ -906,7 +906,7 @@ def run_ours(a):
                        "l2": "flushed between timed steps (256 MB write, outside the events)",
                        "parallelism": f"replicas x{world}"},
             "fp32_tflops": achieved, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "ref_gpu": refgpu, "collision_phase": collision, "large_n": large, "sweep": sweep, "serve": serve, "clocks": clk, "gpu_launches": 13 * a.steps,
+            "ref_gpu": refgpu, "collision_phase": collision, "large_n": large, "sweep": sweep, "serve": serve, "clocks": clk, "gpu_launches": 14 * a.steps,
             "wall_s_timed_region": t_wall, "state_finite": state_ok,
             "step_ms_min_max": [min(step_ms), max(step_ms)],
         }
