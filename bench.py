@@ -878,8 +878,9 @@ def run_ours(a):
                                "FFMA chains per thread) on this GPU in this run, lowest of 12 "
                                "back-to-back runs; MEASURED_PEAKS.json has no FP32 figure",
                 "nominal_peak": info["sm_count"] * 128 * 2 * 2.07e9 / 1e12,
-                "kernel": f"gi::force_kernel<{ipt},KAHAN,STEP> (fused force + kick-drift), "
-                          f"one launch per step via gi_step_pingpong",
+                "kernel": f"gi::force_kernel<{ipt},KAHAN,SUM> (far field; the contact pass runs "
+                          f"beside it on a second stream, then gi::finish_kernel adds the "
+                          f"corrections and the kick-drift), one step per gi_step_pingpong call",
                 "flop_per_interaction": FLOP_PER_INTERACTION,
                 "interactions_per_launch": inter}
         cpu = None
