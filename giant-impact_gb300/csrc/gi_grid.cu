@@ -776,16 +776,17 @@ __device__ __forceinline__ float box_gap2(float3 ilo, float3 ihi, float3 jlo, fl
 // staged bodies and for the 4-byte j-side sums alike.
 __device__ __forceinline__ int swz(int k) { return ((k & 3) << 5) | (k >> 2); }
 
-// Items come from a queue, longest first.  For an item the CTA holds up to 128 bodies
-// of the bucket b (one per thread, all in one cell), stages the neighbour
-// bucket nb in shared memory 128 bodies at a time, and each thread
-// collects the tile slots within r2 < 1 of its body before evaluating the
-// contact law on those alone.  A warp skips each staged block of 32 bodies
-// whose bounding box is provably out of reach of its own bodies' box.
-// When nb is tiled too, each pair is evaluated once for both bodies: the
-// item covers nb's tiles from the chunk's own slots on (all of them when
-// nb != b; within the chunk's own tile only slots above the thread's), and
-// the staged bodies' sums are flushed with 64-bit atomics once per tile.
+// Items come from a queue, longest first.  For an item the CTA holds up to
+// 128 bodies of the bucket b (one per thread, all in one cell), stages the
+// neighbour bucket nb in shared memory 128 bodies at a time, and each
+// thread collects the tile slots within r2 < 1 of its body before
+// evaluating the contact law on those alone.  A warp skips each staged
+// block of 32 bodies whose bounding box is provably out of reach of its own
+// bodies' box.  When nb is tiled too, each pair is evaluated once for both
+// bodies: the item covers nb's tiles from the chunk's own slots on (all of
+// them when nb != b; within the chunk's own tile only slots above the
+// thread's), and the staged bodies' shared sums go into their corrections
+// with 64-bit global atomics once per tile.
 __global__ void __launch_bounds__(128)
 contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ svel,
                     const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
