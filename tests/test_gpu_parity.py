@@ -307,6 +307,37 @@ def test_batch_invariance(gi, torch_cuda, ctx):
         assert np.array_equal(alone[:, :3], mixed[o:o + s, :3]), k
 
 
+def test_side_by_side_and_serial_paths_agree(gi, torch_cuda, ctx):
+    """Tables of fewer than 2^34 pairs run the contact pass beside the far
+    field and finish in a separate kernel; larger ones run it first and take
+    the fused epilogue.  Three 80,000-body runs (6.4e9 pairs each) alone take
+    the first path, batched (1.9e10 pairs) the second: forces and a fused step
+    agree bit for bit."""
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    n = 80000
+    bodies = [gi.ic_lattice(40 + k, n, vel_sigma=1.0) for k in range(3)]
+    pos = np.concatenate([b[0] for b in bodies])
+    vel = np.concatenate([b[1] for b in bodies])
+    runs = [wl.run_desc(gi, k * n, n, bodies[k][2]) for k in range(3)]
+    assert 3 * n * n >= 1 << 34 > n * n
+    batched = gpu_forces(gi, torch, ctx, pos, vel, runs, p)
+    s = stream(torch)
+    dp, dv = dev(torch, pos), dev(torch, vel)
+    ctx.step(dp.data_ptr(), dv.data_ptr(), runs, p, 1, s)
+    torch.cuda.synchronize()
+    for k in range(3):
+        one = [wl.run_desc(gi, 0, n, bodies[k][2])]
+        alone = gpu_forces(gi, torch, ctx, bodies[k][0], bodies[k][1], one, p)
+        assert np.array_equal(alone[:, :3], batched[k * n:(k + 1) * n, :3]), k
+        ap, av = dev(torch, bodies[k][0]), dev(torch, bodies[k][1])
+        ctx.step(ap.data_ptr(), av.data_ptr(), one, p, 1, s)
+        torch.cuda.synchronize()
+        assert np.array_equal(host(ap), host(dp)[k * n:(k + 1) * n]), k
+        assert np.array_equal(host(av), host(dv)[k * n:(k + 1) * n]), k
+
+
 @pytest.mark.parametrize("ipt,jchunk", [(1, 0), (2, 1024), (4, 2048), (4, 128), (1, 512), (8, 256)])
 def test_decompositions_agree(gi, orc, torch_cuda, ctx, ipt, jchunk):
     p = config1_params(gi)
