@@ -71,3 +71,21 @@ def test_sum_of_256_terms_mod_2_32():
         hs = h.sum(axis=1) % 2 ** 32
         ls = l.sum(axis=1) % 2 ** 32
         assert np.array_equal(value(hs, ls, 256), exact(x).sum(axis=1))
+
+
+def test_pair_term_is_the_exact_negation():
+    """A pair of two crowded cells is evaluated once: body j receives the
+    negation of body i's rounded term.  Body j's own evaluation would round
+    -x (dp and dv change sign exactly, the coefficient is symmetric), so the
+    negation must equal round(-x), ties included."""
+    rng = np.random.default_rng(13)
+    x = np.concatenate([
+        (rng.uniform(-1, 1, size=200000) * 2.0 ** rng.uniform(-2, 44, size=200000)),
+        np.arange(-64, 65) * 0.5,                       # every tie near zero
+        (np.arange(-64, 65) + 0.5) * 2.0 ** 22,         # ties at the largest fractional binade
+    ]).astype(np.float32)
+    x = x[np.abs(x) < LIMIT]
+    h, l = split(x)
+    hn, ln = split(-x)
+    assert np.array_equal(-value(h, l, 1), value(hn, ln, 1))
+    assert np.array_equal(-value(h, l, 1), exact(-x))
