@@ -36,7 +36,7 @@ PKG = os.path.join(ROOT, "giant-impact_gb300")
 sys.path.insert(0, PKG)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-FLOP_PER_INTERACTION = 20  # conventional N-body count (SURVEY: sub 3, r2 3, rsqrt, scale 4, FMA 3x2)
+FLOP_PER_INTERACTION = 20  # conventional N-body count: 3 sub, r2 3, rsqrt, scale 4, 3 FMA x 2
 N_TARGET, N_IMPACTOR = 60000, 6000
 
 
