@@ -33,7 +33,7 @@ struct SplatCam {
     float near_plane, far_plane;
     float half_w, half_h;  // width / 2, height / 2
     int width, height, point_size;
-    unsigned int rgb[4];   // Fe body 1, Fe body 2, Si body 1, Si body 2
+    unsigned int rgb[6];   // Fe body 1, Fe body 2, Si body 1, Si body 2, Earth, Moon
     int b0, b1, b2;
 };
 
@@ -42,11 +42,22 @@ __device__ __forceinline__ float dot_rn(const float a[3], float x, float y, floa
     return __fadd_rn(__fadd_rn(__fmul_rn(a[0], x), __fmul_rn(a[1], y)), __fmul_rn(a[2], z));
 }
 
+// scope == nullptr: every element, coloured by origin and material.
+// Otherwise the analysis picture: only elements of scope 1 (Earth, blue)
+// and 2 (Moon, white).
 __global__ void __launch_bounds__(256)
-splat_kernel(const float4 *__restrict__ pos, int n, const __grid_constant__ SplatCam cam,
-             unsigned long long *__restrict__ zbuf)
+splat_kernel(const float4 *__restrict__ pos, int n, const unsigned char *__restrict__ scope,
+             const __grid_constant__ SplatCam cam, unsigned long long *__restrict__ zbuf)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int c;
+        if (scope) {
+            const int sc = scope[i];
+            if (sc != 1 && sc != 2) continue;
+            c = 3 + sc;
+        } else {
+            c = i < cam.b0 ? 0 : (i < cam.b1 ? 1 : (i < cam.b2 ? 2 : 3));
+        }
         const float4 p = pos[i];
         const float dx = __fsub_rn(p.x, cam.eye[0]), dy = __fsub_rn(p.y, cam.eye[1]),
                     dz = __fsub_rn(p.z, cam.eye[2]);
@@ -60,7 +71,6 @@ splat_kernel(const float4 *__restrict__ pos, int n, const __grid_constant__ Spla
         const float wy = __fmul_rn(__fsub_rn(1.0f, yn), cam.half_h);
         const float lo = 0.5f * (float)cam.point_size - 0.5f;
         const int x0 = (int)floorf(__fsub_rn(wx, lo)), y0 = (int)floorf(__fsub_rn(wy, lo));
-        const int c = i < cam.b0 ? 0 : (i < cam.b1 ? 1 : (i < cam.b2 ? 2 : 3));
         const unsigned long long key =
             ((unsigned long long)__float_as_uint(depth) << 32) | cam.rgb[c];
         for (int yy = y0; yy < y0 + cam.point_size; ++yy) {
@@ -132,10 +142,13 @@ extern "C" int gi_view_basis(const gi_view *v, float out[12])
     return GI_OK;
 }
 
-extern "C" int gi_splat(gi_ctx *ctx, const float *pos, int n, const int bounds[3],
-                        const gi_view *view, unsigned char *rgb, void *stream)
+namespace {
+
+// gi_splat (bounds, scope == nullptr) and gi_splat_scope (scope, bounds == nullptr).
+int splat_impl(gi_ctx *ctx, const float *pos, int n, const int *bounds,
+               const unsigned char *scope, const gi_view *view, unsigned char *rgb, void *stream)
 {
-    if (!ctx || !bounds || !view || !rgb || n < 0 || (n > 0 && !pos))
+    if (!ctx || (!bounds && !scope) || !view || !rgb || n < 0 || (n > 0 && !pos))
         return gi_internal_fail(GI_ERR_INVALID_ARG, "gi_splat: NULL argument or n < 0");
     if (view->width <= 0 || view->height <= 0 || view->width > 16384 || view->height > 16384 ||
         view->point_size < 1 || view->point_size > 64)
@@ -166,9 +179,11 @@ extern "C" int gi_splat(gi_ctx *ctx, const float *pos, int n, const int bounds[3
     cam.rgb[1] = pack_rgb(1.0, 0.0, 0.0);     // ColorBody2Core
     cam.rgb[2] = pack_rgb(0.39, 0.26, 0.13);  // ColorBody1Mantle
     cam.rgb[3] = pack_rgb(0.71, 0.40, 0.11);  // ColorBody2Mantle
-    cam.b0 = bounds[0];
-    cam.b1 = bounds[1];
-    cam.b2 = bounds[2];
+    cam.rgb[4] = pack_rgb(0.0, 0.0, 1.0);     // Earth (drawAnalysisPicture)
+    cam.rgb[5] = pack_rgb(1.0, 1.0, 1.0);     // Moon
+    cam.b0 = bounds ? bounds[0] : 0;
+    cam.b1 = bounds ? bounds[1] : 0;
+    cam.b2 = bounds ? bounds[2] : 0;
     const int dev = gi_internal_ctx_device(ctx);
     int prev = -1;
     cudaGetDevice(&prev);
@@ -191,7 +206,7 @@ extern "C" int gi_splat(gi_ctx *ctx, const float *pos, int n, const int bounds[3
         if ((e = cudaMemsetAsync(zbuf, 0xff, npix * 8, s)) != cudaSuccess) break;
         if (n > 0)
             gi::splat_kernel<<<std::min((n + 255) / 256, 8192), 256, 0, s>>>(
-                reinterpret_cast<const float4 *>(pos), n, cam, zbuf);
+                reinterpret_cast<const float4 *>(pos), n, scope, cam, zbuf);
         gi::resolve_kernel<<<(int)std::min<size_t>((npix + 255) / 256, 8192), 256, 0, s>>>(zbuf, npix,
                                                                                           img);
         if ((e = cudaGetLastError()) != cudaSuccess) break;
@@ -202,6 +217,22 @@ extern "C" int gi_splat(gi_ctx *ctx, const float *pos, int n, const int bounds[3
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_status(e, "gi_splat");
     return GI_OK;
+}
+
+}  // namespace
+
+extern "C" int gi_splat(gi_ctx *ctx, const float *pos, int n, const int bounds[3],
+                        const gi_view *view, unsigned char *rgb, void *stream)
+{
+    if (!bounds) return gi_internal_fail(GI_ERR_INVALID_ARG, "gi_splat: bounds is NULL");
+    return splat_impl(ctx, pos, n, bounds, nullptr, view, rgb, stream);
+}
+
+extern "C" int gi_splat_scope(gi_ctx *ctx, const float *pos, int n, const unsigned char *scope,
+                              const gi_view *view, unsigned char *rgb, void *stream)
+{
+    if (!scope) return gi_internal_fail(GI_ERR_INVALID_ARG, "gi_splat_scope: scope is NULL");
+    return splat_impl(ctx, pos, n, nullptr, scope, view, rgb, stream);
 }
 
 extern "C" int gi_write_ppm(const char *path, const unsigned char *rgb, int width, int height)

@@ -265,6 +265,7 @@ _SIGS = {
                       _P], C.c_int),
     "gi_view_basis": ([C.POINTER(View), C.POINTER(C.c_float)], C.c_int),
     "gi_splat": ([_P, _P, C.c_int, C.POINTER(C.c_int), C.POINTER(View), _P, _P], C.c_int),
+    "gi_splat_scope": ([_P, _P, C.c_int, _P, C.POINTER(View), _P, _P], C.c_int),
     "gi_write_ppm": ([C.c_char_p, _P, C.c_int, C.c_int], C.c_int),
     "gi_render_frames": ([C.c_int, C.c_char_p, C.c_char_p, C.POINTER(View), C.c_int, C.c_char_p,
                           C.POINTER(C.c_longlong)], C.c_int),
@@ -801,6 +802,16 @@ def splat(ctx: "Context", pos, n, bounds, v: View, stream=0):
     img = np.zeros((v.height, v.width, 3), np.uint8)
     bd = (C.c_int * 3)(*bounds)
     check(lib().gi_splat(ctx.h, pos, n, bd, C.byref(v), img.ctypes.data, stream))
+    return img
+
+
+def splat_scope(ctx: "Context", pos, n, scope, v: View, stream=0):
+    """The analysis picture: only Earth (scope 1, blue) and Moon (scope 2,
+    white) elements.  pos, scope: device pointers (scope: n bytes, as
+    find_earth_moon writes them).  Returns a (height, width, 3) uint8 image."""
+    import numpy as np
+    img = np.zeros((v.height, v.width, 3), np.uint8)
+    check(lib().gi_splat_scope(ctx.h, pos, n, scope, C.byref(v), img.ctypes.data, stream))
     return img
 
 

@@ -678,6 +678,14 @@ int gi_view_basis(const gi_view *view, float out[12]);
 int gi_splat(gi_ctx *ctx, const float *pos, int n, const int bounds[3], const gi_view *view,
              unsigned char *rgb, void *stream);
 
+/* The analysis picture (drawAnalysisPicture, impactBasicFunctions.h:736-781,
+ * its points): only the elements of scope 1 (Earth, blue) and 2 (Moon,
+ * white) of the device byte array `scope`, as gi_find_earth_moon writes it,
+ * splatted like gi_splat.  The reference's centre-of-mass markers and
+ * angular-momentum lines are not drawn. */
+int gi_splat_scope(gi_ctx *ctx, const float *pos, int n, const unsigned char *scope,
+                   const gi_view *view, unsigned char *rgb, void *stream);
+
 /* Binary PPM (P6) of an rgb image. */
 int gi_write_ppm(const char *path, const unsigned char *rgb, int width, int height);
 

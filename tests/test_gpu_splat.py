@@ -79,3 +79,42 @@ def test_render_frames_to_ppm(gi, torch_cuda, tmp_path):
         img = gi.splat(ctx, d.data_ptr(), n, bounds, v)
         assert raw[len(head):] == img.tobytes()
     ctx.close()
+
+
+def test_analysis_splat_matches_restatement(gi, torch_cuda):
+    """gi_splat_scope draws only Earth (scope 1, blue) and Moon (scope 2,
+    white) elements, pixel for pixel as the restatement; fed by the GPU
+    grouping, the two largest clumps come out blue and white."""
+    torch = torch_cuda
+    n = 20000
+    pos = _scene(2, n)
+    scope = np.random.default_rng(5).integers(0, 4, size=n).astype(np.uint8)
+    v = gi.view((30.0, 20.0, 70.0), up=(0.0, 1.0, 0.0), width=320, height=240, point_size=2)
+    ctx = gi.Context(0)
+    d, ds = torch.from_numpy(pos).cuda(), torch.from_numpy(scope).cuda()
+    img = gi.splat_scope(ctx, d.data_ptr(), n, ds.data_ptr(), v)
+    want = so.splat(pos, None, gi.view_basis(v), v.near_plane, v.far_plane, v.frustum_half,
+                    v.width, v.height, v.point_size, scope=scope)
+    assert np.array_equal(img, want)
+    colours = {tuple(c) for c in img.reshape(-1, 3)}
+    assert colours <= {(0, 0, 0), (0, 0, 255), (255, 255, 255)}
+    assert {(0, 0, 255), (255, 255, 255)} <= colours
+
+    from test_groups_cpu import clumps
+    cp = clumps(3, [900, 300, 40], spacing=1.2, far=25.0)
+    m = len(cp)
+    dc = torch.from_numpy(cp).cuda()
+    sc = torch.zeros(m, dtype=torch.uint8, device="cuda")
+    group = torch.zeros(m, dtype=torch.int32, device="cuda")
+    em = gi.find_earth_moon(ctx, dc.data_ptr(), m, 1.5, [m // 5, 2 * m // 5, 3 * m // 5],
+                            group.data_ptr(), sc.data_ptr())
+    assert em.n_earth == 900 and em.n_moon == 300
+    v2 = gi.view((25.0, 5.0, 120.0), center=(25.0, 5.0, 0.0), up=(0.0, 1.0, 0.0), width=320,
+                 height=240, point_size=2)
+    img2 = gi.splat_scope(ctx, dc.data_ptr(), m, sc.data_ptr(), v2)
+    want2 = so.splat(cp, None, gi.view_basis(v2), v2.near_plane, v2.far_plane, v2.frustum_half,
+                     v2.width, v2.height, v2.point_size, scope=sc.cpu().numpy())
+    assert np.array_equal(img2, want2)
+    c2 = {tuple(c) for c in img2.reshape(-1, 3)}
+    assert {(0, 0, 255), (255, 255, 255)} <= c2
+    ctx.close()
