@@ -237,11 +237,17 @@ struct DeviceGuard {
 // Scratch owned per stream, so that launches on different streams of one
 // context never share a work queue, tickets or partial sums.
 struct StreamScratch {
-    unsigned int *tickets = nullptr;  // per i-block split tickets (zero between launches)
+    // One allocation of counters: [0..1] the persistent kernel's work queue,
+    // then one split ticket per i-block.  All of them are cleared on the
+    // stream before every far-field launch, so a launch that was cut short
+    // (an aborted kernel, a capture torn down) cannot leave the next one a
+    // queue that skips work.
+    unsigned int *counters = nullptr;
+    unsigned int *queue = nullptr;    // counters + 0
+    unsigned int *tickets = nullptr;  // counters + 2
     size_t tickets_cap = 0;
     double *partials = nullptr;       // split-j partial sums
     size_t partials_cap = 0;          // doubles
-    unsigned int *queue = nullptr;    // persistent-kernel work queue (2 counters)
     float4 *pp_pos = nullptr, *pp_vel = nullptr;  // second state buffer of gi_step
     size_t pp_cap = 0;                // bodies
     unsigned int *grid_work = nullptr;  // cell grid of the contact pass (gi_grid.cu)
@@ -258,7 +264,7 @@ struct StreamScratch {
 struct gi_ctx {
     int device = 0;
     int sm_count = 0;
-    gi_options opt{GI_SEP_REF_INT, GI_ACCUM_KAHAN, 0};
+    gi_options opt{GI_SEP_REF_INT, GI_ACCUM_KAHAN, 0, 0};
     bool forced = false;
     gi_tuning forced_tuning{0, 0};
     // Tuned i-bodies per thread per N bucket (floor(log2 n)); 0 = default.
@@ -303,9 +309,8 @@ static void ctx_free(gi_ctx *c)
     DeviceGuard g(c->device);
     for (auto &kv : c->scratch) {
         StreamScratch &x = kv.second;
-        cudaFree(x.tickets);
+        cudaFree(x.counters);
         cudaFree(x.partials);
-        cudaFree(x.queue);
         cudaFree(x.pp_pos);
         cudaFree(x.pp_vel);
         cudaFree(x.grid_work);
@@ -353,6 +358,7 @@ extern "C" int gi_ctx_set_options(gi_ctx *c, const gi_options *o)
     if (o->accum < GI_ACCUM_KAHAN || o->accum > GI_ACCUM_FP64)
         return fail(GI_ERR_INVALID_ARG, "accum %d", o->accum);
     if (o->dense_min < 0) return fail(GI_ERR_INVALID_ARG, "dense_min %d", o->dense_min);
+    if (o->cluster_tries < 0) return fail(GI_ERR_INVALID_ARG, "cluster_tries %d", o->cluster_tries);
     c->opt = *o;
     return GI_OK;
 }
@@ -450,6 +456,7 @@ struct Plan {
     std::vector<LaunchTable> tables;
     std::vector<int> ipt;
     std::vector<long long> bodies;  // bodies in each table's runs
+    std::vector<size_t> ticks;      // split tickets of each table
     size_t tickets = 0;   // max over tables (tables run one after another)
     size_t partials = 0;  // doubles, max over tables
     int max_end = 0;      // largest offset + n
@@ -541,6 +548,7 @@ static int make_plan(const gi_ctx *c, const gi_run *runs, int nruns,
         plan.tables.push_back(t);
         plan.ipt.push_back(p);
         plan.bodies.push_back(nb);
+        plan.ticks.push_back((size_t)tick);
         plan.tickets = std::max(plan.tickets, (size_t)tick);
         plan.partials = std::max(plan.partials, (size_t)part);
     }
@@ -564,15 +572,11 @@ static int ensure_scratch(gi_ctx *c, const Plan &plan, cudaStream_t s, StreamScr
     for (long long b : plan.bodies) gwords = std::max(gwords, gi_grid_words(plan.max_end, b));
     const bool grow_g = gwords > x.grid_work_cap;
     const bool grow_d = (size_t)plan.max_end > x.delta_cap;
-    if (!grow_t && !grow_p && !grow_g && !grow_d && x.queue && x.aux) return GI_OK;
+    if (!grow_t && !grow_p && !grow_g && !grow_d && x.counters && x.aux) return GI_OK;
     if (stream_capturing(s))
         return fail(GI_ERR_INVALID_ARG,
                     "scratch must grow (run once outside stream capture before capturing)");
     GI_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-    if (!x.queue) {
-        GI_CUDA(cudaMalloc(&x.queue, 2 * sizeof(unsigned int)), "cudaMalloc queue");
-        GI_CUDA(cudaMemset(x.queue, 0, 2 * sizeof(unsigned int)), "cudaMemset queue");
-    }
     if (!x.aux) {
         int lo = 0, hi = 0;  // hi: the greatest priority (numerically lowest)
         GI_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi), "cudaDeviceGetStreamPriorityRange");
@@ -581,13 +585,15 @@ static int ensure_scratch(gi_ctx *c, const Plan &plan, cudaStream_t s, StreamScr
         GI_CUDA(cudaEventCreateWithFlags(&x.ev_fork, cudaEventDisableTiming), "cudaEventCreate");
         GI_CUDA(cudaEventCreateWithFlags(&x.ev_join, cudaEventDisableTiming), "cudaEventCreate");
     }
-    if (grow_t) {
-        cudaFree(x.tickets);
-        x.tickets = nullptr;
+    if (grow_t || !x.counters) {
+        cudaFree(x.counters);
+        x.counters = x.queue = x.tickets = nullptr;
         x.tickets_cap = 0;
         size_t cap = std::max(plan.tickets, (size_t)1024);
-        GI_CUDA(cudaMalloc(&x.tickets, cap * sizeof(unsigned int)), "cudaMalloc tickets");
-        GI_CUDA(cudaMemset(x.tickets, 0, cap * sizeof(unsigned int)), "cudaMemset tickets");
+        GI_CUDA(cudaMalloc(&x.counters, (cap + 2) * sizeof(unsigned int)), "cudaMalloc counters");
+        GI_CUDA(cudaMemset(x.counters, 0, (cap + 2) * sizeof(unsigned int)), "cudaMemset counters");
+        x.queue = x.counters;
+        x.tickets = x.counters + 2;
         x.tickets_cap = cap;
     }
     if (grow_p) {
@@ -672,6 +678,11 @@ static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, i
         }
         const int p = plan.ipt[t];
         const int occ = c->occ[c->opt.accum][p];
+        // The queue and this table's tickets start at zero (the kernel also
+        // re-arms them on the way out; this covers a launch that never got
+        // there).  Captured with the launch when the stream is capturing.
+        GI_CUDA(cudaMemsetAsync(x->counters, 0, (2 + plan.ticks[t]) * sizeof(unsigned int), s),
+                "cudaMemsetAsync counters");
         if (pairs >= kOverlapMaxPairs) {
             GI_CUDA(gi_launch_contacts(pos, vel, tab, plan.bodies[t], plan.max_end, x->grid_work,
                                        x->delta, c->sm_count, s),
@@ -1058,6 +1069,24 @@ extern "C" int gi_potential_fp64(gi_ctx *c, const float *pos, const gi_run *runs
     return GI_OK;
 }
 
+extern "C" int gi_debug_fill_counters(gi_ctx *c, void *stream, unsigned int value)
+{
+    if (!c) return fail(GI_ERR_INVALID_ARG, "ctx is NULL");
+    auto it = c->scratch.find((cudaStream_t)stream);
+    if (it == c->scratch.end() || !it->second.counters)
+        return fail(GI_ERR_INVALID_ARG, "no force scratch on this stream yet");
+    DeviceGuard g(c->device);
+    StreamScratch &x = it->second;
+    const size_t words = x.tickets_cap + 2;
+    const unsigned char b = (unsigned char)(value & 0xffu);
+    if (value != 0x01010101u * b)
+        return fail(GI_ERR_INVALID_ARG, "value must repeat one byte (a memset pattern)");
+    GI_CUDA(cudaMemsetAsync(x.counters, b, words * sizeof(unsigned int), (cudaStream_t)stream),
+            "cudaMemsetAsync");
+    GI_CUDA(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
+    return GI_OK;
+}
+
 extern "C" int gi_measure_ffma_peak(int device, double *tflops)
 {
     if (!tflops) return fail(GI_ERR_INVALID_ARG, "tflops is NULL");
@@ -1263,6 +1292,11 @@ extern "C" int gi_graph_destroy(gi_graph *gr)
 int gi_internal_fail(int status, const char *msg) { return fail(status, "%s", msg); }
 
 int gi_internal_ctx_device(gi_ctx *c) { return c ? c->device : -1; }
+
+int gi_internal_ctx_cluster_tries(gi_ctx *c)
+{
+    return (c && c->opt.cluster_tries > 0) ? c->opt.cluster_tries : (1 << 22);
+}
 
 int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d)
 {

@@ -23,8 +23,9 @@
 //      atomicMax of (size << 32 | ~name);
 //   5. tag: scope byte (1 Earth, 2 Moon) and the origin counts.
 // Every loop is bounded: a failed link moves to a strictly smaller index, so
-// a link takes at most N tries; the kernels still stop after a fixed number
-// and raise an error flag that the host turns into GI_ERR_TIMEOUT.
+// a link takes at most N tries; the kernels still stop after a set number
+// (gi_options.cluster_tries, 2^22 by default) and raise an error flag that
+// the host turns into GI_ERR_TIMEOUT.
 #include <algorithm>
 #include <cstdint>
 #include <cstdio>
@@ -33,8 +34,6 @@
 #include "gi_internal.h"
 
 namespace gi {
-
-constexpr int kClusterTries = 1 << 22;
 
 __device__ __forceinline__ int cluster_cell(float x, double inv_cell)
 {
@@ -106,9 +105,9 @@ __device__ __forceinline__ int find_root_ro(const int *parent, int x)
     }
 }
 
-__device__ __forceinline__ bool link(int *parent, int a, int b)
+__device__ __forceinline__ bool link(int *parent, int a, int b, int tries)
 {
-    for (int t = 0; t < kClusterTries; ++t) {
+    for (int t = 0; t < tries; ++t) {
         a = find_root(parent, a);
         b = find_root(parent, b);
         if (a == b) return true;
@@ -132,7 +131,7 @@ __device__ __forceinline__ bool touching(float4 a, float4 b, float touch)
 __global__ void __launch_bounds__(256)
 cluster_union(const float4 *__restrict__ pos, int n, const unsigned int *__restrict__ cursor,
               const int *__restrict__ sorted, unsigned int mask, double inv_cell, float touch,
-              int *parent, int *__restrict__ err)
+              int tries, int *parent, int *__restrict__ err)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -153,7 +152,7 @@ cluster_union(const float4 *__restrict__ pos, int n, const unsigned int *__restr
             const int j = sorted[s];
             if (j <= i) continue;
             if (!touching(pi, pos[j], touch)) continue;
-            if (!link(parent, i, j)) atomicExch(err, 1);
+            if (!link(parent, i, j, tries)) atomicExch(err, 1);
         }
     }
 }
@@ -296,7 +295,9 @@ extern "C" int gi_find_earth_moon(gi_ctx *ctx, const float *pos, int n, float to
         gi::cluster_scatter<<<gridded, 256, 0, s>>>(n, keys, cursor, sorted);
         // cursor[b] is now the end of bucket b
         gi::cluster_union<<<blocks, 256, 0, s>>>(reinterpret_cast<const float4 *>(pos), n, cursor,
-                                                 sorted, m - 1, inv_cell, touch, parent, &res->err);
+                                                 sorted, m - 1, inv_cell, touch,
+                                                 gi_internal_ctx_cluster_tries(ctx), parent,
+                                                 &res->err);
         gi::cluster_flatten<<<gridded, 256, 0, s>>>(parent, n, size, &res->ngroups);
         gi::cluster_pick<<<gridded, 256, 0, s>>>(parent, size, n, nullptr, &res->keys[0]);
         gi::cluster_pick<<<gridded, 256, 0, s>>>(parent, size, n, &res->keys[0], &res->keys[1]);

@@ -343,7 +343,7 @@ __device__ __forceinline__ void flush_slot(unsigned int (*js)[128], int t, int j
 // contacts a body) stay on the warp path.  Either bound is at least
 // kDenseFloor, which bounds the item count.  Bucket state bits: 1 = mixed
 // cells (stays on the warp path), 2 = tiled.
-constexpr unsigned int kDenseFloor = 32;
+// (kDenseFloor itself lives in gi_internal.h: it sizes the scratch.)
 constexpr unsigned int kMixed = 1u, kTiled = 2u;
 
 __host__ __device__ __forceinline__ unsigned int dense_hi(unsigned int dmin)
@@ -552,13 +552,14 @@ __device__ __forceinline__ int run_of_body(const LaunchTable &tab, int i)
 // The cost class is the number of 128-body tiles the item stages, minus
 // one, capped at kItemClasses - 1; pair: nb is tiled too (each pair is
 // evaluated once for both bodies); self: nb == b.
-constexpr unsigned int kItemClasses = 16;
+// (kItemClasses lives in gi_internal.h.)
 
-// Counters of the tiled path, in one block cleared per pass: item count,
-// tiled-bucket count, queue head, then the items per cost class and the
-// fill of each class while ordering.
+// Counters of the tiled path, in one block of kCtrWords words cleared per
+// pass: item count, tiled-bucket count, queue head, then the items per cost
+// class and the fill of each class while ordering.
 constexpr int kCtrItems = 0, kCtrTiled = 1, kCtrHead = 2, kCtrClass = 4,
-              kCtrFill = 4 + (int)kItemClasses, kCtrWords = 4 + 2 * (int)kItemClasses;
+              kCtrFill = 4 + (int)kItemClasses;
+static_assert(kCtrFill + (int)kItemClasses == kCtrWords, "tiled-path counter block");
 
 // Pass 2, one thread per bucket: a crowded bucket of one cell (see
 // dense_hi, dense_lo) becomes tiled and is listed in tiled[0 .. *ntiled).
@@ -912,38 +913,7 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
 
 }  // namespace gi
 
-// Buckets of the grid for `bodies` bodies: a power of two >= 2 * bodies.
-unsigned int gi_grid_buckets(long long bodies)
-{
-    unsigned long long m = 1024;
-    while (m < 2ull * (unsigned long long)bodies) m <<= 1;
-    return (unsigned int)m;
-}
-
-// Tiled-path work items: at most 27 per chunk of 128 bodies of a dense
-// bucket, and a dense bucket holds at least kDenseFloor bodies, so at most
-// 27 (bodies / 128 + bodies / kDenseFloor + 2).
-static size_t dense_item_capacity(long long bodies)
-{
-    return 27 * ((size_t)bodies / 128 + (size_t)bodies / gi::kDenseFloor + 2);
-}
-
-// Tiled buckets: each holds at least kDenseFloor bodies.
-static size_t dense_bucket_capacity(long long bodies)
-{
-    return (size_t)bodies / gi::kDenseFloor + 1;
-}
-
-// Slot-ordered positions and velocities (float4, 8 words per slot); keys
-// (indexed by global body index) and sorted (by slot): max_end words each;
-// cursor and bucket state: one word per bucket each; block sums: 8192; the
-// tiled path's counters and up to 3 words to align the items to 16 bytes;
-// items as listed and as ordered (4 words each); tiled buckets.
-size_t gi_grid_words(long long max_end, long long bodies)
-{
-    return 8 * (size_t)bodies + 2 * (size_t)max_end + 2 * (size_t)gi_grid_buckets(bodies) + 8192 +
-           gi::kCtrWords + 3 + 8 * dense_item_capacity(bodies) + dense_bucket_capacity(bodies);
-}
+// gi_grid_buckets and gi_grid_words (the scratch layout) are in gi_internal.h.
 
 cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, cudaStream_t s)
 {
@@ -974,7 +944,7 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     unsigned int *ntiled = ctr + gi::kCtrTiled;
     uint4 *raw = reinterpret_cast<uint4 *>((reinterpret_cast<uintptr_t>(ctr + gi::kCtrWords) + 15) &
                                            ~static_cast<uintptr_t>(15));
-    const size_t icap = dense_item_capacity(bodies);
+    const size_t icap = gi_dense_item_capacity(bodies);
     uint4 *items = raw + icap;
     unsigned int *tiled = reinterpret_cast<unsigned int *>(items + icap);
     int maxn = 0;
@@ -998,7 +968,7 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
     gi::dense_mark_kernel<<<std::min((int)((m + 255) / 256), 4 * nsm), 256, 0, s>>>(
         pos, tab, cursor, sorted, m, m - 1, dmin, state, tiled, ntiled);
     gi::dense_sort_kernel<<<2 * nsm, 256, 0, s>>>(pos, vel, cursor, sorted, spos, svel, tiled, ntiled);
-    const int gt = (int)std::min<size_t>((dense_bucket_capacity(bodies) + 7) / 8, 4 * (size_t)nsm);
+    const int gt = (int)std::min<size_t>((gi_dense_bucket_capacity(bodies) + 7) / 8, 4 * (size_t)nsm);
     gi::dense_items_kernel<<<gt, 256, 0, s>>>(pos, tab, cursor, sorted, m - 1, state, tiled, ctr,
                                               raw);
     const int go = (int)std::min<size_t>((icap + 255) / 256, 4 * (size_t)nsm);

@@ -91,9 +91,53 @@ cudaError_t gi_launch_finish(int epi, const ForceArgs &a, const LaunchTable &tab
                              int nsm, cudaStream_t s);
 
 // gi_grid.cu: contact corrections of every body of the table's runs into
-// delta (3 x int64 per body) through a hashed cell grid.
-unsigned int gi_grid_buckets(long long bodies);
-size_t gi_grid_words(long long max_end, long long bodies);
+// delta (3 x int64 per body) through a hashed cell grid.  Its scratch layout
+// is computed here, as constexpr functions, so that gi_noalloc.cu can check
+// at compile time that its static array holds the largest run it accepts.
+namespace gi {
+// A bucket goes through the tiled path only when it holds at least this many
+// bodies; that bounds the number of tiled buckets and work items.
+constexpr unsigned int kDenseFloor = 32;
+// Cost classes of the tiled path's work items (128-body tiles staged - 1).
+constexpr unsigned int kItemClasses = 16;
+// Tiled-path counters: items, tiled buckets, queue head, one spare, then a
+// count and a fill cursor per cost class.
+constexpr int kCtrWords = 4 + 2 * (int)kItemClasses;
+}  // namespace gi
+
+// Buckets of the grid for `bodies` bodies: a power of two >= 2 * bodies.
+constexpr unsigned int gi_grid_buckets(long long bodies)
+{
+    unsigned long long m = 1024;
+    while (m < 2ull * (unsigned long long)bodies) m <<= 1;
+    return (unsigned int)m;
+}
+
+// Tiled-path work items: at most 27 per chunk of 128 bodies of a dense
+// bucket, and a dense bucket holds at least kDenseFloor bodies, so at most
+// 27 (bodies / 128 + bodies / kDenseFloor + 2).  Tiled buckets: each holds at
+// least kDenseFloor bodies.
+constexpr size_t gi_dense_item_capacity(long long bodies)
+{
+    return 27 * ((size_t)bodies / 128 + (size_t)bodies / gi::kDenseFloor + 2);
+}
+constexpr size_t gi_dense_bucket_capacity(long long bodies)
+{
+    return (size_t)bodies / gi::kDenseFloor + 1;
+}
+
+// Words of grid scratch: slot-ordered positions and velocities (float4, 8
+// words per slot); keys (indexed by global body index) and sorted (by slot):
+// max_end words each; cursor and bucket state: one word per bucket each;
+// block sums: 8192; the tiled path's counters and up to 3 words to align the
+// items to 16 bytes; items as listed and as ordered (4 words each); tiled
+// buckets.
+constexpr size_t gi_grid_words(long long max_end, long long bodies)
+{
+    return 8 * (size_t)bodies + 2 * (size_t)max_end + 2 * (size_t)gi_grid_buckets(bodies) + 8192 +
+           gi::kCtrWords + 3 + 8 * gi_dense_item_capacity(bodies) +
+           gi_dense_bucket_capacity(bodies);
+}
 cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const LaunchTable &tab,
                                long long bodies, int max_end, unsigned int *work,
                                long long *delta, int nsm, cudaStream_t s);
@@ -120,6 +164,8 @@ int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d
 long long gi_internal_scratch_bytes(gi_ctx *ctx, int n);
 // Device ordinal of a context (-1 for NULL).
 int gi_internal_ctx_device(gi_ctx *ctx);
+// Attempts one union-find link of gi_find_earth_moon may make (gi_options).
+int gi_internal_ctx_cluster_tries(gi_ctx *ctx);
 // gi_grid.cu: exclusive scan of m <= 1024 * 8192 counters in place; sums
 // holds 8192 words of scratch.
 cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, cudaStream_t s);

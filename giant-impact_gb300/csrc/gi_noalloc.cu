@@ -26,7 +26,12 @@
 // Host code cannot use the array's name as a device address (on the host it
 // names a stand-in object).  The device address is obtained once per device
 // with cudaGetSymbolAddress, with that device current, by the first call on
-// that device; make that first call before any stream capture.
+// that device; make that first call before any stream capture.  The address
+// is remembered together with the identity of the device's CUDA context, so
+// after a cudaDeviceReset (a new context, where the array may lie elsewhere)
+// the next call looks it up again; make that call outside capture too.
+#include <cuda.h>
+
 #include <cstring>
 #include <mutex>
 
@@ -47,34 +52,11 @@ constexpr size_t kCountersBytes = 4096;
 constexpr size_t kDeltaOff = kCountersBytes;  // 3 x int64 per body
 constexpr size_t kGridOff = kDeltaOff + 3 * sizeof(long long) * kMaxBodies;
 
-size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-
-std::mutex g_mu;
-void *g_base[64] = {nullptr};
-
-// Device address of g_noalloc_scratch on the current device (set-up on the
-// first call per device).
-int scratch_base(void **out)
-{
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return gi_internal_fail(GI_ERR_CUDA, "cudaGetDevice failed");
-    if (dev < 0 || dev >= 64) return gi_internal_fail(GI_ERR_NO_DEVICE, "device index out of range");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_base[dev]) {
-        void *ptr = nullptr;
-        e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return gi_internal_fail(GI_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed");
-        g_base[dev] = ptr;
-    }
-    *out = g_base[dev];
-    return GI_OK;
-}
+constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Chunks per i-block for a run of T tiles with big chunks of 2^kLg tiles
 // (the layout the force kernel decodes, see tail_tiles).
-int nsplit_for(int T)
+constexpr int nsplit_for(int T)
 {
     if ((1 << kLg) >= T) return 1;
     int r = 0;
@@ -85,6 +67,85 @@ int nsplit_for(int T)
         ++r;
     }
     return r;
+}
+
+// The carve of the static array for a run of n bodies: counters, contact
+// corrections, the cell grid, then the split-j partial sums (sized for the
+// largest split).  Every part grows with n, so the largest run accepted is
+// the one to check; it is checked here, at compile time, so that a change of
+// the grid's layout or of the split cannot leave maximum-size calls refused.
+constexpr int tiles_for(size_t n) { return (int)((n + GI_NT - 1) / GI_NT); }
+constexpr int iblocks_for(size_t n) { return (int)((n + GI_NT * kIpt - 1) / (GI_NT * kIpt)); }
+constexpr size_t part_off_for(size_t n)
+{
+    return kGridOff + align256(gi_grid_words((long long)n, (long long)n) * sizeof(unsigned int));
+}
+constexpr size_t kPartBytes = (size_t)kMaxSplit * 3 * sizeof(double) * kMaxBodies;
+static_assert(nsplit_for(tiles_for(kMaxBodies)) <= kMaxSplit,
+              "the largest run splits into more j-chunks than the partial sums hold");
+static_assert(part_off_for(kMaxBodies) + kPartBytes <= GI_NOALLOC_BYTES,
+              "the static scratch does not hold the largest run");
+static_assert(2 * sizeof(unsigned int) + iblocks_for(kMaxBodies) * sizeof(unsigned int) <=
+                  kCountersBytes,
+              "the counter block does not hold the largest run's tickets");
+
+std::mutex g_mu;
+void *g_base[64] = {nullptr};
+unsigned long long g_ctx_id[64] = {0};
+
+// Identity of the calling thread's current CUDA context (0 if none is
+// current or the driver does not say).  The driver calls are looked up
+// through the runtime, so libgi does not link against the driver library.
+unsigned long long current_context_id()
+{
+    typedef CUresult (*GetCurrent)(CUcontext *);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        looked_up = true;
+        void *f = nullptr, *g = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q1) ==
+                cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &g, 12000, cudaEnableDefault, &q2) ==
+                cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<GetCurrent>(f);
+            get_id = reinterpret_cast<GetId>(g);
+        }
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c) return 0;
+    if (get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of g_noalloc_scratch on the current device: looked up on
+// the first call per device, and again when the device's context is a new
+// one (after a device reset).  With no context identity to go by it is
+// looked up on every call.
+int scratch_base(void **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return gi_internal_fail(GI_ERR_CUDA, "cudaGetDevice failed");
+    if (dev < 0 || dev >= 64) return gi_internal_fail(GI_ERR_NO_DEVICE, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_mu);
+    const unsigned long long id = current_context_id();
+    if (!g_base[dev] || id == 0 || id != g_ctx_id[dev]) {
+        void *ptr = nullptr;
+        e = cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return gi_internal_fail(GI_ERR_CUDA, "cudaGetSymbolAddress of the static scratch failed");
+        g_base[dev] = ptr;
+        g_ctx_id[dev] = current_context_id();  // the lookup made the context current
+    }
+    *out = g_base[dev];
+    return GI_OK;
 }
 
 }  // namespace
@@ -130,11 +191,10 @@ extern "C" int gi_forces_collision_noalloc(const float *pos, const float *vel, f
     tab.sep_test = GI_SEP_REF_INT;
     tab.dense_min = 256;
 
-    // Carve the static array.
-    const size_t grid_bytes = align256(gi_grid_words(n, n) * sizeof(unsigned int));
-    const size_t part_off = kGridOff + grid_bytes;
-    const size_t part_bytes = (size_t)kMaxSplit * 3 * sizeof(double) * kMaxBodies;
-    if (d.nsplit > kMaxSplit || part_off + part_bytes > GI_NOALLOC_BYTES ||
+    // Carve the static array (the largest run is checked to fit at compile
+    // time; this guards the arithmetic at run time as well).
+    const size_t part_off = part_off_for((size_t)n);
+    if (d.nsplit > kMaxSplit || part_off + kPartBytes > GI_NOALLOC_BYTES ||
         2 * sizeof(unsigned int) + (size_t)d.nib * sizeof(unsigned int) > kCountersBytes)
         return gi_internal_fail(GI_ERR_BAD_SIZE, "static scratch layout does not fit this run");
     void *base = nullptr;

@@ -72,6 +72,7 @@ struct gi_server {
     long long interactions = 0;
     long long rounds = 0;
     long long completed = 0;
+    long long cancelled = 0;
 };
 
 namespace {
@@ -430,6 +431,27 @@ extern "C" int gi_server_fetch(gi_server *s, long long id, float *pos_host, floa
     return GI_OK;
 }
 
+extern "C" int gi_server_cancel(gi_server *s, long long id)
+{
+    if (!s) return gi_internal_fail(GI_ERR_INVALID_ARG, "server is NULL");
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return gi_internal_fail(GI_ERR_INVALID_ARG, "unknown request id");
+    Req &q = it->second;
+    if (q.state == GI_REQ_QUEUED) {
+        s->queue.erase(std::find(s->queue.begin(), s->queue.end(), id));
+    } else if (q.state == GI_REQ_LIVE) {
+        // Between rounds nothing of this server is in flight (every round
+        // ends with a stream synchronisation), so the range can be handed
+        // back at once; the other live runs' ranges are not touched.
+        s->live.erase(std::find(s->live.begin(), s->live.end(), id));
+        pool_free(s, q.offset, q.run.n);
+        s->bytes_in_use -= q.bytes;
+    }
+    s->reqs.erase(it);
+    ++s->cancelled;
+    return GI_OK;
+}
+
 extern "C" int gi_server_get_stats(gi_server *s, gi_server_stats *out)
 {
     if (!s || !out) return gi_internal_fail(GI_ERR_INVALID_ARG, "NULL argument");
@@ -440,5 +462,6 @@ extern "C" int gi_server_get_stats(gi_server *s, gi_server_stats *out)
     out->bytes_in_use = s->bytes_in_use;
     out->pool_bodies = s->cap;
     out->interactions = s->interactions;
+    out->cancelled = s->cancelled;
     return GI_OK;
 }

@@ -47,7 +47,8 @@ class Run(C.Structure):
 
 
 class Options(C.Structure):
-    _fields_ = [("sep_test", C.c_int), ("accum", C.c_int), ("dense_min", C.c_int)]
+    _fields_ = [("sep_test", C.c_int), ("accum", C.c_int), ("dense_min", C.c_int),
+                ("cluster_tries", C.c_int)]
 
 
 class Tuning(C.Structure):
@@ -95,7 +96,8 @@ class RequestInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("live", C.c_int), ("queued", C.c_int), ("completed", C.c_longlong),
                 ("rounds", C.c_longlong), ("bytes_in_use", C.c_longlong),
-                ("pool_bodies", C.c_longlong), ("interactions", C.c_longlong)]
+                ("pool_bodies", C.c_longlong), ("interactions", C.c_longlong),
+                ("cancelled", C.c_longlong)]
 
 
 class SetupGenerating(C.Structure):
@@ -213,6 +215,7 @@ _SIGS = {
     "gi_run_host": ([_P, _P, _P, C.c_int, C.POINTER(Run), C.c_int, C.POINTER(PairParams),
                      C.c_int, C.c_int, _P], C.c_int),
     "gi_measure_ffma_peak": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
+    "gi_debug_fill_counters": ([_P, _P, C.c_uint], C.c_int),
     "gi_server_create": ([C.c_int, C.POINTER(ServerConfig), C.POINTER(PairParams), C.c_int,
                           C.POINTER(_P)], C.c_int),
     "gi_server_destroy": ([_P], C.c_int),
@@ -221,6 +224,7 @@ _SIGS = {
     "gi_server_query": ([_P, C.c_longlong, C.POINTER(RequestInfo)], C.c_int),
     "gi_server_fetch": ([_P, C.c_longlong, _P, _P], C.c_int),
     "gi_server_get_stats": ([_P, C.POINTER(ServerStats)], C.c_int),
+    "gi_server_cancel": ([_P, C.c_longlong], C.c_int),
     "gi_params_from_material": ([C.c_double] * 10 + [C.POINTER(PairParams)], C.c_int),
     "gi_params_from_collision_consts": ([C.POINTER(ForceCollisionConsts), C.POINTER(PairParams)],
                                         C.c_int),
@@ -393,11 +397,11 @@ class Context:
     """Owns a gi_ctx (scratch, options, tuning) on one device."""
 
     def __init__(self, device: int = 0, sep_test: int = GI_SEP_REF_INT,
-                 accum: int = GI_ACCUM_KAHAN, dense_min: int = 0):
+                 accum: int = GI_ACCUM_KAHAN, dense_min: int = 0, cluster_tries: int = 0):
         h = C.c_void_p()
         check(lib().gi_ctx_create(C.byref(h), device))
         self.h = h
-        self.set_options(sep_test, accum, dense_min)
+        self.set_options(sep_test, accum, dense_min, cluster_tries)
 
     def close(self):
         if self.h:
@@ -410,9 +414,15 @@ class Context:
         except Exception:
             pass
 
-    def set_options(self, sep_test=GI_SEP_REF_INT, accum=GI_ACCUM_KAHAN, dense_min=0):
-        o = Options(sep_test, accum, dense_min)
+    def set_options(self, sep_test=GI_SEP_REF_INT, accum=GI_ACCUM_KAHAN, dense_min=0,
+                    cluster_tries=0):
+        o = Options(sep_test, accum, dense_min, cluster_tries)
         check(lib().gi_ctx_set_options(self.h, C.byref(o)))
+
+    def fill_counters(self, value: int, stream=0):
+        """Test hook: overwrite the work-queue counters and split tickets of
+        this stream's scratch with a memset byte pattern."""
+        check(lib().gi_debug_fill_counters(self.h, stream, value))
 
     def set_tuning(self, i_per_thread=None, jchunk=0):
         if i_per_thread is None:
@@ -548,6 +558,9 @@ class Server:
         vel = np.zeros((n, 4), np.float32)
         check(lib().gi_server_fetch(self.h, rid, pos.ctypes.data, vel.ctypes.data))
         return pos, vel
+
+    def cancel(self, rid):
+        check(lib().gi_server_cancel(self.h, rid))
 
     def stats(self) -> ServerStats:
         st = ServerStats()

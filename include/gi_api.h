@@ -160,6 +160,10 @@ typedef struct gi_options {
                               or of a quarter of it next to such a cell, take
                               the shared-memory tiled path; 0 = 256.
                               Results do not depend on it. */
+    int cluster_tries;     /* gi_find_earth_moon: attempts one union-find
+                              link may make (each failed attempt moves to a
+                              strictly smaller root) before the call gives
+                              up with GI_ERR_TIMEOUT; 0 = 2^22. */
 } gi_options;
 
 /* Work decomposition of one run (chosen per N bucket by the autotuner or
@@ -330,6 +334,13 @@ int gi_run_host(gi_ctx *ctx, float *pos_host, float *vel_host, int ntotal,
  * ~50 ms microbenchmark): the denominator of the force kernel's roofline. */
 int gi_measure_ffma_peak(int device, double *tflops);
 
+/* Test hook (no counterpart in the reference): overwrites the work-queue
+ * counters and split tickets of the context's scratch for `stream` with a
+ * memset byte pattern (value = 0xbbbbbbbb for byte bb), as a launch that was
+ * cut short would leave them; synchronous.  The next force call must still
+ * be correct, because every launch clears them first. */
+int gi_debug_fill_counters(gi_ctx *ctx, void *stream, unsigned int value);
+
 /* ------------------------------------------------------------------------ */
 /* Serving loop (continuous batching of impact runs)                        */
 /* ------------------------------------------------------------------------ */
@@ -379,6 +390,7 @@ typedef struct gi_server_stats {
     long long bytes_in_use;
     long long pool_bodies;       /* capacity of the device state pool */
     long long interactions;      /* pair interactions computed so far */
+    long long cancelled;         /* requests withdrawn by gi_server_cancel */
 } gi_server_stats;
 
 typedef struct gi_server gi_server;
@@ -397,6 +409,12 @@ int gi_server_query(gi_server *srv, long long id, gi_server_request_info *info);
 /* Copies a finished run's bodies out and forgets the request. */
 int gi_server_fetch(gi_server *srv, long long id, float *pos_host, float *vel_host);
 int gi_server_get_stats(gi_server *srv, gi_server_stats *out);
+/* Withdraws a request in any state, between rounds: a queued request leaves
+ * the queue; a live run gives back its slot, its device range and its share
+ * of the budget at once (the other live runs are not touched); a finished
+ * result is discarded.  The id is forgotten.  GI_ERR_INVALID_ARG for an
+ * unknown id. */
+int gi_server_cancel(gi_server *srv, long long id);
 
 /* ------------------------------------------------------------------------ */
 /* Parameter helpers (host only)                                            */

@@ -14,10 +14,13 @@ import subprocess
 import numpy as np
 import pytest
 
+import build_ref
 import formats_oracle as fo
 from conftest import ROOT
 
-REF = "/root/reference/Code"
+# The reference's Code/ folder (GI_REFERENCE_DIR, see oracle/build_ref.py);
+# the tests that read its sources skip where it is absent.
+REF = os.path.join(build_ref.reference_dir() or "/nonexistent", "Code")
 
 # Setup files in the reference's layout (a comment line without '=', then
 # "Name = value;"), written for these tests.

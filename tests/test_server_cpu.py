@@ -124,3 +124,43 @@ def test_shortest_remaining_work_first(gi, params):
     assert [srv2.query(i).steps_done for i in ids] == [0, 10, 10]
     with pytest.raises(gi.GIError):
         gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=10**9, policy=7)
+
+
+def test_cancel_frees_slot_and_budget(gi, params):
+    """A cancelled request gives its slot and budget back at once: a live
+    run's range returns to the pool, a queued request leaves the queue, and
+    the others keep their exact step counts."""
+    n = 1000
+    per_run = 2 * 2 * 16 * n
+    srv = gi.Server(params, device=gi.SERVER_DRY_RUN, budget_bytes=2 * per_run, max_live_runs=2,
+                    steps_per_round=10)
+    a, b, c, d = (srv.submit(*bodies(n, k), run(gi, n), 30) for k in range(4))
+    srv.round()
+    assert [srv.query(i).state for i in (a, b, c, d)] == [gi.REQ_LIVE, gi.REQ_LIVE,
+                                                          gi.REQ_QUEUED, gi.REQ_QUEUED]
+    srv.cancel(a)                      # live: slot, range and budget come back now
+    st = srv.stats()
+    assert (st.live, st.queued, st.bytes_in_use, st.cancelled) == (1, 2, per_run, 1)
+    with pytest.raises(gi.GIError):
+        srv.query(a)                   # forgotten
+    srv.cancel(d)                      # queued: leaves the queue
+    assert srv.stats().queued == 1
+    srv.round()                        # c takes a's slot
+    assert srv.query(c).state == gi.REQ_LIVE
+    assert srv.query(b).steps_done == 20 and srv.query(c).steps_done == 10
+    while srv.stats().live:
+        srv.round()
+    assert srv.query(b).steps_done == 30 and srv.query(c).steps_done == 30
+    st = srv.stats()
+    assert (st.completed, st.cancelled, st.bytes_in_use) == (2, 2, 0)
+    srv.cancel(b)                      # a finished result is discarded
+    with pytest.raises(gi.GIError):
+        srv.fetch(b, n)
+    with pytest.raises(gi.GIError) as e:
+        srv.cancel(12345)              # unknown id
+    assert e.value.status == 1  # GI_ERR_INVALID_ARG
+    # the pool ranges handed back are reused: a fresh pair fits where a and b were
+    e1, e2 = (srv.submit(*bodies(n, 9 + k), run(gi, n), 5) for k in range(2))
+    srv.round()
+    assert srv.query(e1).state == gi.REQ_DONE and srv.query(e2).state == gi.REQ_DONE
+    assert srv.stats().pool_bodies <= 65536
