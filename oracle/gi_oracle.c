@@ -483,6 +483,93 @@ void gio_count_flips(const float *pos, const float *vel, const int *idx,
     out[1] = sep_flips;
 }
 
+/* ------------------------------------------------------ FP64 trajectory -- */
+
+static void fp64_log(const double *X, const double *V, const double *m, int n, int nfe,
+                     const gio_params *c, double *out, int nt)
+{
+    double ke = 0.0, pe = 0.0, lx = 0.0, ly = 0.0, lz = 0.0, px = 0.0, py = 0.0, pz = 0.0;
+    #pragma omp parallel for schedule(dynamic, 16) num_threads(nt) reduction(+ : pe)
+    for (int i = 0; i < n; ++i) {
+        double u = 0.0;
+        for (int j = 0; j < n; ++j) {
+            if (j == i) continue;
+            double dx = X[3 * j] - X[3 * i], dy = X[3 * j + 1] - X[3 * i + 1],
+                   dz = X[3 * j + 2] - X[3 * i + 2];
+            double r = sqrt(dx * dx + dy * dy + dz * dz);
+            double g, kk, krm, kri;
+            class_consts((i < nfe) + (j < nfe), c, &g, &kk, &krm, &kri);
+            if (r >= 1.0) u += -g / r;
+            else u += -g + g * (r - 1.0) - kk * (r - r * r * r / 3.0 - 2.0 / 3.0);
+        }
+        pe += u;
+    }
+    for (int i = 0; i < n; ++i) {
+        const double *x = X + 3 * i, *v = V + 3 * i;
+        ke += 0.5 * m[i] * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+        lx += m[i] * (x[1] * v[2] - x[2] * v[1]);
+        ly += m[i] * (x[2] * v[0] - x[0] * v[2]);
+        lz += m[i] * (x[0] * v[1] - x[1] * v[0]);
+        px += m[i] * v[0]; py += m[i] * v[1]; pz += m[i] * v[2];
+    }
+    out[0] = ke + 0.5 * pe;
+    out[1] = lx; out[2] = ly; out[3] = lz;
+    out[4] = px; out[5] = py; out[6] = pz;
+}
+
+void gio_integrate_fp64(double *X, double *V, int n, int nfe, const gio_params *c,
+                        double dt, int nsteps, int every, double *log, int sep_test,
+                        int nthreads)
+{
+    int nt = pick_threads(nthreads);
+    double *F = (double *)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
+    double *m = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < n; ++i) m[i] = (i < nfe) ? (double)c->MassFe : (double)c->MassSi;
+    int rec = 0;
+    if (every > 0) fp64_log(X, V, m, n, nfe, c, log + 7 * rec++, nt);
+    for (int step = 1; step <= nsteps; ++step) {
+        #pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+        for (int i = 0; i < n; ++i) {
+            double fx = 0.0, fy = 0.0, fz = 0.0;
+            const double xi = X[3 * i], yi = X[3 * i + 1], zi = X[3 * i + 2];
+            for (int j = 0; j < n; ++j) {
+                if (j == i) continue;
+                double dx = X[3 * j] - xi, dy = X[3 * j + 1] - yi, dz = X[3 * j + 2] - zi;
+                double r2 = dx * dx + dy * dy + dz * dz;
+                double r = sqrt(r2);
+                int test = (i < nfe) + (j < nfe);
+                double g, k, krm, kri;
+                class_consts(test, c, &g, &k, &krm, &kri);
+                int band = band_f64(test, r, c), sep = 0;
+                if (band >= 2) {
+                    double dpdv = dx * (V[3 * j] - V[3 * i]) + dy * (V[3 * j + 1] - V[3 * i + 1]) +
+                                  dz * (V[3 * j + 2] - V[3 * i + 2]);
+                    sep = (sep_test == GIO_SEP_SIGN) ? (dpdv > 0.0) : (dpdv >= 1.0);
+                }
+                double s;
+                if (band == 0) {
+                    s = g / (r2 * r);
+                } else {
+                    double kk = band == 1 ? k : (sep ? (band == 2 ? krm : kri) : k);
+                    s = (g - kk * (1.0 - r2)) / r;
+                }
+                fx += s * dx; fy += s * dy; fz += s * dz;
+            }
+            F[3 * i] = fx; F[3 * i + 1] = fy; F[3 * i + 2] = fz;
+        }
+        for (int i = 0; i < n; ++i) {
+            const double dtm = dt / m[i];
+            for (int a = 0; a < 3; ++a) {
+                V[3 * i + a] += F[3 * i + a] * dtm;
+                X[3 * i + a] += V[3 * i + a] * dt;
+            }
+        }
+        if (every > 0 && step % every == 0) fp64_log(X, V, m, n, nfe, c, log + 7 * rec++, nt);
+    }
+    free(F);
+    free(m);
+}
+
 /* ------------------------------------------------------------- groups -- */
 
 static inline int touching_ref(const f4 *P, int k, int j, float touch)

@@ -107,6 +107,18 @@ void gio_count_flips(const float *pos, const float *vel, const int *idx,
                      int nidx, long long *out, const gio_run *runs, int nruns,
                      const gio_params *params, int sep_test, int nthreads);
 
+/* FP64 trajectory of one run: the pair law in double, with double band and
+ * separation decisions, on double positions and velocities (x, y, z per
+ * body), integrated nsteps with the reference's kick-drift
+ * (impactAddTime.cu:379-394) in double: v += F dt / m, then x += v dt.
+ * Masses MassFe (the first nfe bodies) and MassSi.  At step 0 and every
+ * `every` steps, log[7 k .. 7 k + 6] receives E = kinetic + pair potential
+ * (the potential of gio_potential_fp64), L = sum m x cross v and
+ * P = sum m v (x, y, z).  pos3 and vel3 are updated in place. */
+void gio_integrate_fp64(double *pos3, double *vel3, int n, int nfe,
+                        const gio_params *params, double dt, int nsteps, int every,
+                        double *log, int sep_test, int nthreads);
+
 /* Groups of touching bodies, restated literally from findEarthAndMoon
  * (Code/ImpactCode/impactBasicFunctions.h:109-155): group numbers are the
  * index of the body that started each group, the FP32 distance is

@@ -56,6 +56,7 @@ def lib() -> C.CDLL:
         L.gio_potential_fp64.argtypes = [P, P, I, P, P, I, P, I]
         L.gio_diag_fp64.argtypes = [P, P, P, I, P, P, P]
         L.gio_count_flips.argtypes = [P, P, P, I, P, P, I, P, I, I]
+        L.gio_integrate_fp64.argtypes = [P, P, I, I, P, D, I, I, P, I, I]
         L.gio_r2_threshold.argtypes = [F]
         L.gio_groups_ref.argtypes = [P, I, F, P]
         L.gio_groups_uf.argtypes = [P, I, F, P]
@@ -185,6 +186,38 @@ def count_flips(pos, vel, idx, runs, params, sep_test=SEP_REF_INT, nthreads=0):
     lib().gio_count_flips(pos.ctypes.data, vel.ctypes.data, idx.ctypes.data, len(idx),
                           out.ctypes.data, ra, nr, _params_arr(params), sep_test, nthreads)
     return int(out[0]), int(out[1])
+
+
+def integrate_fp64(pos, vel, nfe, params, dt, nsteps, every, sep_test=SEP_REF_INT, nthreads=0):
+    """FP64 trajectory of one run (double state, double predicates).
+    Returns (pos (n, 3) float64, vel (n, 3) float64, log (k, 7)) with log
+    rows [E, Lx, Ly, Lz, Px, Py, Pz] at step 0 and every `every` steps."""
+    X = np.ascontiguousarray(np.asarray(pos)[:, :3], dtype=np.float64).copy()
+    V = np.ascontiguousarray(np.asarray(vel)[:, :3], dtype=np.float64).copy()
+    nrec = (nsteps // every + 1) if every > 0 else 0
+    log = np.zeros((max(nrec, 1), 7), np.float64)
+    lib().gio_integrate_fp64(X.ctypes.data, V.ctypes.data, len(X), int(nfe),
+                             _params_arr(params), float(dt), int(nsteps), int(every),
+                             log.ctypes.data, sep_test, nthreads)
+    return X, V, log[:nrec]
+
+
+def material_params(G=1.0, D=1.0, mass_fe=1.0, mass_si=0.4, k_fe=5.0, k_si=1.5, kr_fe=0.02,
+                    kr_si=0.01, sd_fe=0.002, sd_si=0.001) -> dict:
+    """The pair table of loadKernalConstantStructures (impactAddTime.cu:128-170)
+    for a general G and Si mass, computed in double and stored as float."""
+    f = np.float32
+    mix_fe_first = sd_fe >= sd_si
+    return {
+        "GMassFeFe": f(G * mass_fe * mass_fe), "GMassFeSi": f(G * mass_fe * mass_si),
+        "GMassSiSi": f(G * mass_si * mass_si), "KFeFe": f(2.0 * k_fe), "KSiSi": f(2.0 * k_si),
+        "KFeSi": f(k_fe + k_si), "KRFeFe": f(2.0 * k_fe * kr_fe), "KRSiSi": f(2.0 * k_si * kr_si),
+        "KRFeSi": f(k_fe * kr_fe + k_si * kr_si),
+        "KRMix": f(k_fe + k_si * kr_si) if mix_fe_first else f(k_fe * kr_fe + k_si),
+        "ShellBreakFe": f(D - D * sd_fe), "ShellBreakSi": f(D - D * sd_si),
+        "ShellBreakFeSi1": f(D - D * (sd_si if mix_fe_first else sd_fe)),
+        "ShellBreakFeSi2": f(D - D * (sd_fe if mix_fe_first else sd_si)),
+        "MassFe": f(mass_fe), "MassSi": f(mass_si)}
 
 
 def r2_threshold(s: float) -> float:

@@ -248,3 +248,42 @@ def test_oracle_matches_reference_golden(orc, path):
         p2, v2 = orc.move_ref(g["pos"], g["vel"], force, runs)
         assert np.array_equal(v2, g["vel_after"])
         assert np.array_equal(p2, g["pos_after"])
+
+
+def test_material_params_match_library(gi, orc):
+    """The oracle's own pair table (used where the library must not load)
+    equals gi_params_from_material field for field, both orders of the
+    shell depths."""
+    for sd in ((0.002, 0.001), (0.001, 0.002)):
+        a = orc.material_params(1.0, 1.0, 1.0, 0.4, 5.0, 1.5, 0.02, 0.01, *sd)
+        b = gi.params_from_material(1.0, 1.0, 1.0, 0.4, 5.0, 1.5, 0.02, 0.01, *sd)
+        for name in orc.PARAM_FIELDS:
+            assert np.float32(a[name]) == np.float32(getattr(b, name)), name
+
+
+def test_integrate_fp64_first_step_and_invariants(gi, orc):
+    """One step of the FP64 integrator is the FP64 force (double predicates)
+    followed by the double kick-drift; its log holds E = KE + PE, L and P of
+    the state; momentum is conserved (the law is antisymmetric pair by pair)
+    and, with KR = K, energy is conserved to the integrator's order."""
+    pos, vel, nfe = gi.ic_lattice(17, 600, spacing=0.97, jitter=0.01, vel_sigma=0.8)
+    p = config1_params(gi)
+    run = [(0, 600, nfe, 0, 0, 0, 0, 0)]
+    dt = 1e-3
+    X, V, log = orc.integrate_fp64(pos, vel, nfe, p, dt, 1, 1)
+    f64, _ = orc.forces_fp64(pos, vel, run, p, branch=orc.BRANCH_F64)
+    m = np.where(np.arange(600) < nfe, p.MassFe, p.MassSi).astype(np.float64)[:, None]
+    v1 = vel[:, :3].astype(np.float64) + f64 * dt / m
+    x1 = pos[:, :3].astype(np.float64) + v1 * dt
+    assert np.allclose(V, v1, rtol=1e-13, atol=1e-15)
+    assert np.allclose(X, x1, rtol=1e-15, atol=1e-13)
+    d = orc.diag_fp64(pos, vel, run[0], p)
+    pe = orc.potential_fp64(pos, run, p).sum() / 2.0
+    assert abs(log[0, 0] - (d[10] + pe)) <= 1e-12 * abs(log[0, 0])
+    assert np.allclose(log[0, 4:7], d[11:14], rtol=1e-12, atol=1e-12)
+    # conservative control (KR = K): 200 steps
+    q = gi.params_from_material(1.0, 1.0, 1.0, 0.4, 5.0, 1.5, 1.0, 1.0, 0.002, 0.001)
+    _, _, lg = orc.integrate_fp64(pos, vel, nfe, q, dt, 200, 50)
+    scale = np.abs(m[:, 0] * vel[:, :3].astype(np.float64).T).sum()
+    assert np.abs(lg[:, 4:7] - lg[0, 4:7]).max() <= 1e-11 * scale
+    assert np.abs(lg[:, 0] - lg[0, 0]).max() <= 1e-3 * abs(lg[0, 0])
