@@ -644,15 +644,21 @@ static int convert_params(const gi_pair_params *params, int nparams, std::vector
 // uniform balls (default tuning): the side-by-side pass takes 33 % off at
 // n = 8,192, 5 % at 49,152, 2 % at 98,304, and adds 5 % at 131,072.
 constexpr long long kOverlapMaxPairs = 1LL << 34;
+// Far-field CTAs per SM while the contact pass runs beside it.  Measured on
+// the 66,000-body impact (ms per fused step, settled / collision phase):
+// 3 CTAs 1.72 / 2.60, 4: 1.68 / 2.57, 6: 1.68 / 2.59, 8: 1.67 / 2.54; the
+// contact kernels fit beside 8 of them, and more warps keep the far field's
+// FMA pipe busier.
+constexpr int kSideBySideCtas = 8;
 
 // One force evaluation (or fused step) per table.  The contact pass and the
 // far field are independent until the epilogue, so for tables of fewer than
 // kOverlapMaxPairs pairs they run side by side: the contact pass on the
 // scratch's aux stream, forked from the caller's stream; the far field on
-// the caller's stream with half its resident CTAs per SM (at that size it
-// runs as fast at half occupancy and leaves room on every SM for the contact
-// kernels); then, joined, the epilogue, with the fused epilogue's
-// arithmetic.  Either way the results are the same bits.
+// the caller's stream with kSideBySideCtas resident CTAs per SM (at that
+// size it runs as fast as at full occupancy and leaves room on every SM for
+// the contact kernels); then, joined, the epilogue, with the fused
+// epilogue's arithmetic.  Either way the results are the same bits.
 static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, int epi,
                           const float4 *pos, const float4 *vel, float4 *force,
                           float4 *pos_out, float4 *vel_out, cudaStream_t s)
@@ -698,7 +704,7 @@ static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, i
                 "contact pass");
         GI_CUDA(cudaEventRecord(x->ev_join, x->aux), "cudaEventRecord");
         GI_CUDA(gi_launch_force(p, c->opt.accum, GI_EPI_SUM, a, tab,
-                                c->sm_count * std::max(1, (occ + 1) / 2), s),
+                                c->sm_count * std::min(occ, kSideBySideCtas), s),
                 "force kernel launch");
         GI_CUDA(cudaStreamWaitEvent(s, x->ev_join, 0), "cudaStreamWaitEvent");
         GI_CUDA(gi_launch_finish(epi, a, tab, maxn, c->sm_count, s), "epilogue launch");

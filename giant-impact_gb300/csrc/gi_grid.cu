@@ -208,6 +208,28 @@ __device__ __forceinline__ float contact_coef(const PairRow &w, int sep_test, fl
     return __fmaf_rn(mag, invr, w.far);
 }
 
+// contact_coef with j's velocity read (from shared memory) only for pairs
+// inside the shell band, where the separation test needs it.  Same
+// arithmetic, same result.
+__device__ __forceinline__ float contact_coef_at(const PairRow &w, int sep_test, float dx,
+                                                 float dy, float dz, float r2, float4 vi,
+                                                 const float4 *vj)
+{
+    float K = w.K;
+    if (!(r2 >= w.Tband)) {
+        const float4 v = *vj;
+        const float dvx = __fsub_rn(v.x, vi.x), dvy = __fsub_rn(v.y, vi.y),
+                    dvz = __fsub_rn(v.z, vi.z);
+        const float dpdv = __fmaf_rn(dz, dvz, __fmaf_rn(dx, dvx, __fmul_rn(dy, dvy)));
+        const bool sep = (sep_test == GI_SEP_SIGN) ? (dpdv > 0.0f) : (dpdv >= 1.0f);
+        if (sep) K = (r2 >= w.Tmid) ? w.KRmid : w.KRin;
+    }
+    const float mag = contact_mag(w.G, K, r2);
+    float invr = rsqrt_mufu(r2);
+    invr = invr * __fmaf_rn(-0.5f * r2 * invr, invr, 1.5f);
+    return __fmaf_rn(mag, invr, w.far);
+}
+
 // Fixed-point sums without the FP64 unit.  Each pair term x (FP32, in
 // units of the fixed point) is rounded to the nearest integer, ties to
 // even, exactly as cvt.rni.s64.f32 would; that instruction issues on the
@@ -262,19 +284,41 @@ __device__ __forceinline__ void fix_fold(FixSum3 &a)
     a.hx = a.hy = a.hz = a.lx = a.ly = a.lz = a.n = 0u;
 }
 
-// Adds round(c dx), round(c dy), round(c dz).  Terms out of the split's
-// range (a pair at r ~ 0, or NaN) take the hardware conversion.
-__device__ __forceinline__ void fix_add3(FixSum3 &a, float c, float dx, float dy, float dz)
+// The split is exact for every term of a pair with a normal r2: there
+// 1 / r is finite, |d| <= r (up to rounding), so |c d| <= (|mag| + G m m) /
+// unit <= 2^40 (1 + 2^-16) < kFixMax, the fixed-point unit being
+// (2 Gmax + Kmax) 2^-40.  Coincident bodies (r2 = 0), a denormal r2 (the
+// MUFU rsqrt flushes it to zero) or NaN take the hardware conversion,
+// which rounds the same way; so the choice never changes a result.
+__device__ __forceinline__ bool fix_in_range(float r2) { return r2 >= 0x1p-126f; }
+
+// Adds round(c dx), round(c dy), round(c dz) for a pair of squared
+// distance r2 (see fix_in_range); x and y in packed FP32x2 instructions,
+// with the roundings of fix_split (s = fl(t + M); lo = fl(t - fl(s - M)),
+// here as fma(fl(s - M), -1, t); fl(lo + C)).  FOLD: fold when kFixFold
+// terms are pending (a caller that adds fewer terms between its own folds
+// passes false).
+template <bool FOLD = true>
+__device__ __forceinline__ void fix_add3(FixSum3 &a, float c, float dx, float dy, float dz,
+                                         float r2)
 {
-    const float tx = __fmul_rn(c, dx), ty = __fmul_rn(c, dy), tz = __fmul_rn(c, dz);
-    if (fabsf(tx) < kFixMax && fabsf(ty) < kFixMax && fabsf(tz) < kFixMax) {
-        fix_split(tx, a.hx, a.lx);
-        fix_split(ty, a.hy, a.ly);
+    const float2 txy = __fmul2_rn(make_float2(c, c), make_float2(dx, dy));
+    const float tz = __fmul_rn(c, dz);
+    if (fix_in_range(r2)) {
+        const float2 s = __fadd2_rn(txy, make_float2(kFixM, kFixM));
+        const float2 lo = __ffma2_rn(__fadd2_rn(s, make_float2(-kFixM, -kFixM)),
+                                     make_float2(-1.0f, -1.0f), txy);
+        const float2 l = __fadd2_rn(lo, make_float2(kFixC, kFixC));
+        a.hx += __float_as_uint(s.x);
+        a.hy += __float_as_uint(s.y);
+        a.lx += __float_as_uint(l.x);
+        a.ly += __float_as_uint(l.y);
         fix_split(tz, a.hz, a.lz);
-        if (++a.n == kFixFold) fix_fold(a);
+        ++a.n;
+        if (FOLD && a.n == kFixFold) fix_fold(a);
     } else {
-        a.x += __float2ll_rn(tx);
-        a.y += __float2ll_rn(ty);
+        a.x += __float2ll_rn(txy.x);
+        a.y += __float2ll_rn(txy.y);
         a.z += __float2ll_rn(tz);
     }
 }
@@ -284,27 +328,34 @@ __device__ __forceinline__ void fix_add3(FixSum3 &a, float c, float dx, float dy
 // evaluation would give (dp and dv change sign exactly, c is symmetric, and
 // rounding to nearest even is odd-symmetric), to the shared sums js[.][k]
 // of j's staged slot: true values mod 2^32, hi in js[0..2], lo in js[3..5].
-// A term out of the split's range goes to j's global sums directly.
+// A term out of the split's range goes to j's global sums directly.  The
+// caller folds (at most kFixFold terms between its folds).
 __device__ __forceinline__ void fix_add3_pair(FixSum3 &a, unsigned int (*js)[128], int k,
-                                              long long *dj, float c, float dx, float dy, float dz)
+                                              long long *dj, float c, float dx, float dy, float dz,
+                                              float r2)
 {
-    const float tx = __fmul_rn(c, dx), ty = __fmul_rn(c, dy), tz = __fmul_rn(c, dz);
-    if (fabsf(tx) < kFixMax && fabsf(ty) < kFixMax && fabsf(tz) < kFixMax) {
-        const float t3[3] = {tx, ty, tz};
-        unsigned int *h3[3] = {&a.hx, &a.hy, &a.hz};
-        unsigned int *l3[3] = {&a.lx, &a.ly, &a.lz};
+    const float2 txy = __fmul2_rn(make_float2(c, c), make_float2(dx, dy));
+    const float tz = __fmul_rn(c, dz);
+    if (fix_in_range(r2)) {
+        const float2 s = __fadd2_rn(txy, make_float2(kFixM, kFixM));
+        const float2 lo = __ffma2_rn(__fadd2_rn(s, make_float2(-kFixM, -kFixM)),
+                                     make_float2(-1.0f, -1.0f), txy);
+        const float2 l = __fadd2_rn(lo, make_float2(kFixC, kFixC));
+        const float sz = __fadd_rn(tz, kFixM);
+        const float lz = __fadd_rn(__fsub_rn(tz, __fsub_rn(sz, kFixM)), kFixC);
+        const unsigned int sb[3] = {__float_as_uint(s.x), __float_as_uint(s.y), __float_as_uint(sz)};
+        const unsigned int lb[3] = {__float_as_uint(l.x), __float_as_uint(l.y), __float_as_uint(lz)};
+        a.hx += sb[0]; a.hy += sb[1]; a.hz += sb[2];
+        a.lx += lb[0]; a.ly += lb[1]; a.lz += lb[2];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const float sd = __fadd_rn(t3[d], kFixM);
-            const float ld = __fadd_rn(__fsub_rn(t3[d], __fsub_rn(sd, kFixM)), kFixC);
-            *h3[d] += __float_as_uint(sd);
-            *l3[d] += __float_as_uint(ld);
-            atomicAdd(&js[d][k], __float_as_uint(kFixM) - __float_as_uint(sd));
-            atomicAdd(&js[3 + d][k], __float_as_uint(kFixC) - __float_as_uint(ld));
+            atomicAdd(&js[d][k], __float_as_uint(kFixM) - sb[d]);
+            atomicAdd(&js[3 + d][k], __float_as_uint(kFixC) - lb[d]);
         }
-        if (++a.n == kFixFold) fix_fold(a);
+        ++a.n;
     } else {
-        const long long vx = __float2ll_rn(tx), vy = __float2ll_rn(ty), vz = __float2ll_rn(tz);
+        const long long vx = __float2ll_rn(txy.x), vy = __float2ll_rn(txy.y),
+                        vz = __float2ll_rn(tz);
         a.x += vx;
         a.y += vy;
         a.z += vz;
@@ -416,7 +467,7 @@ __device__ __forceinline__ void contact_body_warp(const float4 *__restrict__ pos
         const float c =
             contact_coef(select_row(j < sw, row_fe, row_si), sep_test, dx, dy, dz, r2, vi, vj) *
             inv_unit;
-        fix_add3(acc, c, dx, dy, dz);
+        fix_add3(acc, c, dx, dy, dz, r2);
     };
     // 64 candidates a pass, two per lane, so that each lane has two
     // independent loads in flight.  Slots within r2 < 1 are queued in the
@@ -777,6 +828,39 @@ __device__ __forceinline__ float box_gap2(float3 ilo, float3 ihi, float3 jlo, fl
 // staged bodies and for the 4-byte j-side sums alike.
 __device__ __forceinline__ int swz(int k) { return ((k & 3) << 5) | (k >> 2); }
 
+// The contact law on one thread's hits of a staged tile (slots my[0 .. nh)),
+// starting at the (lane / 32)-th part of the list so that lanes with alike
+// lists (neighbouring bodies) rarely hit one slot's shared sums at once.
+// PAIR: the pair's j-side term goes to the slot's shared sums too.  MIXED:
+// the tile holds Fe bodies, so the pair-class row is chosen per hit; a tile
+// of Si bodies alone (most of them: Fe is the small core) uses row_si.
+template <bool PAIR, bool MIXED>
+__device__ __forceinline__ void tile_hits(FixSum3 &acc, const unsigned char *my, int nh, int lane,
+                                          const float4 *sp, const float4 *sv,
+                                          unsigned int (*js)[128], long long *delta, float4 pi,
+                                          float4 vi, const PairRow &row_fe, const PairRow &row_si,
+                                          int sw, int sep_test, float inv_unit)
+{
+    const float2 npxy = make_float2(-pi.x, -pi.y);
+    int h = (lane * nh) >> 5;
+    for (int n = 0; n < nh; ++n) {
+        const int k = swz(my[h]);  // shared-memory position of the slot
+        h = h + 1 == nh ? 0 : h + 1;
+        const float4 pj = sp[k];
+        const int j = __float_as_int(pj.w);  // never i: b and nb differ, or k > t
+        const float2 dxy = __fadd2_rn(make_float2(pj.x, pj.y), npxy);
+        const float dx = dxy.x, dy = dxy.y, dz = pj.z - pi.z;
+        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
+        const float c = contact_coef_at(MIXED ? select_row(j < sw, row_fe, row_si) : row_si,
+                                        sep_test, dx, dy, dz, r2, vi, &sv[k]) *
+                        inv_unit;
+        if (PAIR) fix_add3_pair(acc, js, k, delta + 3 * (size_t)j, c, dx, dy, dz, r2);
+        else fix_add3<false>(acc, c, dx, dy, dz, r2);
+    }
+    // at most 128 hits a tile: fold before kFixFold terms can be pending
+    if (acc.n >= kFixFold - 128u) fix_fold(acc);
+}
+
 // Items come from a queue, longest first.  For an item the CTA holds up to
 // 128 bodies of the bucket b (one per thread, all in one cell), stages the
 // neighbour bucket nb in shared memory 128 bodies at a time, and each
@@ -788,7 +872,8 @@ __device__ __forceinline__ int swz(int k) { return ((k & 3) << 5) | (k >> 2); }
 // them when nb != b; within the chunk's own tile only slots above the
 // thread's), and the staged bodies' shared sums go into their corrections
 // with 64-bit global atomics once per tile.
-__global__ void __launch_bounds__(128)
+// 72 registers: 7 CTAs of 128 threads per SM, with no spills.
+__global__ void __maxnreg__(72)
 contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ svel,
                     const unsigned int *__restrict__ cursor, const int *__restrict__ sorted,
                     const unsigned int *__restrict__ state, long long *__restrict__ delta,
@@ -843,9 +928,11 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
             if (t == 0 && base + 128u >= nend) nw = atomicAdd(&ctr[kCtrHead], 1u);
             const unsigned int u = base + (unsigned int)t;
             float3 lo = make_float3(kInf, kInf, kInf), hi = make_float3(-kInf, -kInf, -kInf);
+            bool fe_slot = false;  // the staged body is of the run's Fe core
             if (u < nend) {
                 const int j = sorted[u];
                 if (j >= rbeg && j < rend) {
+                    fe_slot = j < sw;
                     const float4 q = spos[u];
                     sp[tz] = make_float4(q.x, q.y, q.z, __int_as_float(j));
                     sv[tz] = svel[u];
@@ -860,7 +947,8 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
                 blo[warp] = lo;
                 bhi[warp] = hi;
             }
-            __syncthreads();
+            // does any staged body of the run belong to the Fe core?
+            const int mixed = __syncthreads_or(fe_slot);
             if (!valid) continue;
             const int cnt = (int)min(128u, nend - base);
             const int kmin = (self && base == first) ? t + 1 : 0;  // own tile: each pair once
@@ -879,21 +967,20 @@ contact_tile_kernel(const float4 *__restrict__ spos, const float4 *__restrict__ 
                     }
                 }
             }
-            // lanes start at different points of their lists, so that lanes
-            // with alike lists rarely hit one slot's shared sums at once
-            int h = (lane * nh) >> 5;
-            for (int n = 0; n < nh; ++n) {
-                const int k = swz(my[h]);  // shared-memory position of the slot
-                h = h + 1 == nh ? 0 : h + 1;
-                const float4 pj = sp[k];
-                const int j = __float_as_int(pj.w);  // never i: b and nb differ, or k > t
-                const float dx = pj.x - pi.x, dy = pj.y - pi.y, dz = pj.z - pi.z;
-                const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dx, dx, __fmul_rn(dy, dy)));
-                const float c = contact_coef(select_row(j < sw, row_fe, row_si), tab.sep_test, dx,
-                                             dy, dz, r2, vi, sv[k]) *
-                                inv_unit;
-                if (pair) fix_add3_pair(acc, js, k, delta + 3 * (size_t)j, c, dx, dy, dz);
-                else fix_add3(acc, c, dx, dy, dz);
+            if (pair) {
+                if (mixed)
+                    tile_hits<true, true>(acc, my, nh, lane, sp, sv, js, delta, pi, vi, row_fe,
+                                          row_si, sw, tab.sep_test, inv_unit);
+                else
+                    tile_hits<true, false>(acc, my, nh, lane, sp, sv, js, delta, pi, vi, row_fe,
+                                           row_si, sw, tab.sep_test, inv_unit);
+            } else {
+                if (mixed)
+                    tile_hits<false, true>(acc, my, nh, lane, sp, sv, js, delta, pi, vi, row_fe,
+                                           row_si, sw, tab.sep_test, inv_unit);
+                else
+                    tile_hits<false, false>(acc, my, nh, lane, sp, sv, js, delta, pi, vi, row_fe,
+                                            row_si, sw, tab.sep_test, inv_unit);
             }
         }
         __syncthreads();  // the last tile's j-side sums are complete; s_w is read
