@@ -79,6 +79,10 @@ def args_parse():
                     help="steps from the timed state into the collision phase")
     ap.add_argument("--collision-steps", type=int, default=20)
     ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the force-error checks against the FP64 oracle")
+    ap.add_argument("--no-hbm", action="store_true",
+                    help="skip the memory-bound kernels (move, FP64 diagnostics)")
     ap.add_argument("--large-steps", type=int, default=4)
     ap.add_argument("--study", choices=["drift", "precision"], default=None,
                     help="run a study instead of the benchmark (prints one JSON line)")
@@ -175,6 +179,33 @@ class ClockSampler:
 def make_workload(gi, torch, wl, seed, settle_steps):
     pos, vel, nfe = wl.impact(gi, torch, N_TARGET, N_IMPACTOR, seed=seed, settle_steps=settle_steps)
     return pos, vel, nfe
+
+
+STATE_FILE = os.path.join(ROOT, "bench_state", "impact66k_seed2.npz")
+
+
+def load_state():
+    """The settled 66,000-body impact state both arms time (written by
+    bench_state/make_state.py), or None where the file is absent."""
+    import numpy as np
+    if not os.path.exists(STATE_FILE):
+        return None
+    z = np.load(STATE_FILE)
+    return (np.ascontiguousarray(z["pos"], np.float32), np.ascontiguousarray(z["vel"], np.float32),
+            int(z["nfe"]))
+
+
+def bench_config(n, world, advance):
+    """The workload as both arms print it (identical dicts)."""
+    return {"workload": "plain two-body impact: 60,000-body target + 6,000-body impactor, "
+                        "30% Fe, spin 0.5 breakup, 45 deg, 1.2 v_esc, dt 1e-3",
+            "n_bodies": n, "interactions_per_step": n * (n - 1),
+            "state": "bench_state/impact66k_seed2.npz (seed 2, settled 1,500 damped + 150 "
+                     "rest steps)",
+            "advance_steps": advance,
+            "l2": "GPU arm: flushed between timed steps (256 MB write, outside the events); "
+                  "host arm: not applicable",
+            "parallelism": f"replicas x{world}"}
 
 
 def cpu_baseline(orc, pos, vel, nfe, p, seconds):
@@ -497,8 +528,9 @@ def collision_section(torch, ctx, flush, pos_d, vel_d, run, p, a):
     steps timed one by one with CUDA events, L2 flushed between them."""
     n = pos_d.shape[0]
     bufs = [(pos_d.clone(), vel_d.clone()), (torch.empty_like(pos_d), torch.empty_like(vel_d))]
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
     s = stream.cuda_stream
+    torch.cuda.synchronize()
     ctx.step(bufs[0][0].data_ptr(), bufs[0][1].data_ptr(), [run], p, a.collision_advance, s)
 
     def one(k):
@@ -510,16 +542,18 @@ def collision_section(torch, ctx, flush, pos_d, vel_d, run, p, a):
     torch.cuda.synchronize()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(a.collision_steps)]
-    for k in range(a.collision_steps):
-        flush.fill_(float(k))
-        evs[k][0].record(stream)
-        one(3 + k)
-        evs[k][1].record(stream)
+    with torch.cuda.stream(stream):
+        for k in range(a.collision_steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            one(3 + k)
+            evs[k][1].record(stream)
     torch.cuda.synchronize()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
     ms = sum(step_ms) / len(step_ms)
     dp, dv = bufs[(3 + a.collision_steps) % 2]
-    return {"advance_steps": a.collision_advance, "steps": a.collision_steps, "ms_per_step": ms,
+    return {"_state": (dp.cpu().numpy(), dv.cpu().numpy()),
+            "advance_steps": a.collision_advance, "steps": a.collision_steps, "ms_per_step": ms,
             "value": n * (n - 1) / (ms * 1e-3), "unit": "interactions/s",
             "step_ms_min_max": [min(step_ms), max(step_ms)],
             "state_finite": bool(torch.isfinite(dp).all().item() and torch.isfinite(dv).all().item()),
@@ -572,6 +606,150 @@ def large_n_section(gi, torch, wl, ctx, peak_sustained, a):
             "tuning": {"i_per_thread": ipt, "jchunk": jchunk, "autotune_s": round(tune_s, 1)}}
 
 
+def measured_hbm_peak():
+    """HBM copy bandwidth measured on the GB300s, else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "of fallback (6.8 TB/s, an earlier GB300 copy measurement)"
+
+
+def hbm_section(gi, torch, wl, ctx, pos, vel, nfe, p, copies=128, reps=7):
+    """The memory-bound kernels on a state far larger than L2: the settled
+    66,000-body state tiled `copies` times (8,448,000 bodies: pos + vel
+    270 MB, force 135 MB).  Each call is timed alone with CUDA events on the
+    launching stream, L2 flushed (256 MB write) before it, median of `reps`.
+      move: gi_move = one move_kernel launch, the unfused kick-drift
+            (impactAddTime.cu:379-394): 80 B/body (read pos, vel, force;
+            write pos, vel).
+      diag: gi_diag_fp64, scope all = diag_pass1 + diag_pass2 (FP64 mass,
+            centre of mass, momentum, kinetic energy; angular momentum about
+            the centre of mass) + two one-thread finalisers + a 120-byte
+            read-back: 2 x 32 B/body (pos + vel read per pass)."""
+    import numpy as np
+    n = len(pos) * copies
+    P = torch.from_numpy(pos).cuda().repeat(copies, 1)
+    V = torch.from_numpy(vel).cuda().repeat(copies, 1)
+    F = torch.zeros_like(P)
+    F[:, :3] = 1e-3
+    run = wl.run_desc(gi, 0, n, nfe)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    s = stream.cuda_stream
+    peak, peak_src = measured_hbm_peak()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        ts = []
+        for k in range(reps + 2):
+            flush.fill_(float(k))
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if k >= 2:
+                ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts)), [min(ts), max(ts)]
+
+    move_ms, move_mm = timed(lambda: ctx.move(P.data_ptr(), V.data_ptr(), F.data_ptr(), [run], s))
+    diag_ms, diag_mm = timed(lambda: ctx.diag(P.data_ptr(), V.data_ptr(), run, p, stream=s))
+    clk = clocks.stop()
+    out = {"bodies": n, "state": f"settled 66,000-body impact state tiled {copies} times",
+           "hbm_peak_gbs": peak, "peak_source": peak_src, "clocks": clk,
+           "l2": "flushed before every timed call (256 MB write, outside the events)"}
+    for name, ms, mm, per_body, what in (
+            ("move", move_ms, move_mm, 80, "move_kernel (unfused kick-drift), one launch"),
+            ("diag", diag_ms, diag_mm, 64, "gi_diag_fp64 scope all: diag_pass1 + diag_pass2 + "
+                                           "finalisers + 120-byte read-back")):
+        gbs = per_body * n / (ms * 1e-3) / 1e9
+        out[name] = {"ms": ms, "ms_min_max": mm, "algorithmic_bytes": per_body * n,
+                     "bytes_per_body": per_body, "gbs": gbs, "frac_of_hbm": gbs / peak,
+                     "what": what}
+    del P, V, F, flush
+    torch.cuda.empty_cache()
+    return out
+
+
+def accuracy_section(gi, orc, torch, pos, vel, nfe, p, label, ksub=4096, seed=11):
+    """Force error of one force pass on `pos, vel` against the FP64 oracle on a
+    seeded i-subsample of `ksub` bodies against all j: with the reference's
+    FP32 branch decisions (the bar, 1e-5) and with FP64 decisions, the
+    decision flips between the two, the contact pairs of the sample and the
+    median cancellation sum_j |f_ij| / |F_i|; and the reference kernel's
+    error on the same state."""
+    import ctypes as C
+    import numpy as np
+    wl = _load("gi_workloads", os.path.join(PKG, "gi_workloads.py"))
+    n = len(pos)
+    run = [(0, n, nfe, 0, 0, 0, 0, 0)]
+    ctx = gi.Context(torch.cuda.current_device())
+    dp, dv = torch.from_numpy(pos).cuda(), torch.from_numpy(vel).cuda()
+    df = torch.full_like(dp, float("nan"))
+    ctx.forces(dp.data_ptr(), dv.data_ptr(), df.data_ptr(), [wl.run_desc(gi, 0, n, nfe)], p)
+    torch.cuda.synchronize()
+    ctx.close()
+    f = df.cpu().numpy()[:, :3].astype(np.float64)
+    idx = np.sort(np.random.default_rng(seed).choice(n, min(ksub, n), replace=False)).astype(np.int32)
+    t0 = time.perf_counter()
+    f64, absf = orc.forces_fp64(pos, vel, run, p, idx=idx, branch=orc.BRANCH_F32)
+    f64d, _ = orc.forces_fp64(pos, vel, run, p, idx=idx, branch=orc.BRANCH_F64)
+    band, sep = orc.count_flips(pos, vel, idx, run, p)
+    t_oracle = time.perf_counter() - t0
+    contacts = 0
+    for c0 in range(0, len(idx), 256):
+        xi = pos[idx[c0:c0 + 256], None, :3].astype(np.float64)
+        contacts += int((((xi - pos[None, :, :3]) ** 2).sum(-1) < 1.0).sum())
+    contacts -= len(idx)  # the self pairs
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    out = {"state": label, "subsample": len(idx), "pairs_checked": len(idx) * (n - 1),
+           "force_rel_l2": rel(f[idx], f64), "force_rel_l2_fp64_decisions": rel(f[idx], f64d),
+           "bar": 1e-5, "flips": {"band": band, "separation": sep},
+           "contacts_per_body": contacts / len(idx),
+           "median_cancellation": float(np.median(absf / np.maximum(
+               np.linalg.norm(f64, axis=1), 1e-300))),
+           "oracle": f"FP64 pair law (oracle/gi_oracle.c), {orc.max_threads()} threads, "
+                     f"{t_oracle:.1f} s"}
+    ref = orc.ref_lib()
+    if ref is not None:
+        # The reference kernel fixes m_Si = 1, so it runs in its own units:
+        # masses / mu, K / mu^2, velocities / sqrt(mu) (mu = m_Si).  Its
+        # separation test, int inout = dp.dv, is not unit-free, so its error
+        # is taken against the FP64 oracle in those same units.
+        mu = p.MassSi
+        rp = gi.params_from_material(1.0, 1.0, p.MassFe / mu, 1.0, 5.0 / mu**2, 1.5 / mu**2,
+                                     0.02, 0.01, 0.002, 0.001)
+        nr = ((n + 255) // 256) * 256
+        pp = np.zeros((nr, 4), np.float32)
+        vv = np.zeros((nr, 4), np.float32)
+        pp[:n], vv[:n] = pos, vel / np.float32([mu ** 0.5, mu ** 0.5, mu ** 0.5, 1.0])
+        pp[n:, :3] = 1e7 + np.arange(nr - n)[:, None] * 10.0
+        vv[n:, 3] = 1.0
+        rdp, rdv = torch.from_numpy(pp).cuda(), torch.from_numpy(vv).cuda()
+        rdf = torch.zeros_like(rdp)
+        assert ref.giref_forces_collision(rdp.data_ptr(), rdv.data_ptr(), rdf.data_ptr(),
+                                          C.byref(gi.collision_consts(rp, nfe)), nr,
+                                          torch.cuda.current_stream().cuda_stream) == 0
+        torch.cuda.synchronize()
+        rf = rdf.cpu().numpy()[:n, :3].astype(np.float64)
+        rrun = [(0, n, nfe, 0, 0, 0, 0, 0)]
+        rv = np.ascontiguousarray(vv[:n])
+        r64, _ = orc.forces_fp64(pos, rv, rrun, rp, idx=idx, branch=orc.BRANCH_F32)
+        r64d, _ = orc.forces_fp64(pos, rv, rrun, rp, idx=idx, branch=orc.BRANCH_F64)
+        rband, rsep = orc.count_flips(pos, rv, idx, rrun, rp)
+        out["reference_kernel"] = {
+            "force_rel_l2": rel(rf[idx], r64), "force_rel_l2_fp64_decisions": rel(rf[idx], r64d),
+            "flips": {"band": rband, "separation": rsep},
+            "what": f"getForcesCollisionSingleGPU, N padded to {nr}, in its own units (m_Si = 1), "
+                    f"against the FP64 oracle in the same units"}
+    return out
+
+
 def _energy_l(ctx, dp, dv, run, params):
     """FP64 total energy (KE + pair potential), total angular momentum,
     momentum and angular momentum about the centre of mass of one run."""
@@ -618,7 +796,7 @@ def study_drift(a):
     steps = a.study_steps or 20000
     every = a.study_every
     ctx = gi.Context(0, dense_min=a.dense_min)
-    pos, vel, nfe = make_workload(gi, torch, wl, 2, a.settle_steps)
+    pos, vel, nfe = load_state() or make_workload(gi, torch, wl, 2, a.settle_steps)
     n = len(pos)
     kr = 1.0 if a.conservative else None  # KR = K: the contact law is conservative
     m = wl.MATERIAL
@@ -770,10 +948,20 @@ def study_precision(a):
                                           nr, s) == 0
         e1.record()
         torch.cuda.synchronize()
-        f = df.cpu().numpy()[:n] * np.float32(mu ** 2)  # back to config units (F' = F / mu^2)
-        res = errors(f)
+        # In the reference's own units (its int dp.dv separation test is not
+        # unit-free): error against the FP64 oracle evaluated in those units.
+        f = df.cpu().numpy()[:n].astype(np.float64)
+        r64, _ = orc.forces_fp64(pos, np.ascontiguousarray(vv[:n]),
+                                 [(0, n, nfe, 0, 0, 0, 0, 0)], rp, idx=idx)
+        d = f[idx, :3] - r64
+        rscale = np.sqrt((r64 ** 2).sum(1))
+        rel = np.sqrt((d ** 2).sum(1)) / np.maximum(rscale, 1e-300)
+        res = {"rel_l2": float(np.sqrt((d ** 2).sum() / (r64 ** 2).sum())),
+               "median_rel": float(np.median(rel)), "p99_rel": float(np.quantile(rel, 0.99)),
+               "max_rel": float(rel.max())}
         res["force_ms"] = e0.elapsed_time(e1)
-        res["what"] = f"reference getForcesCollisionSingleGPU, N padded to {nr}"
+        res["what"] = (f"reference getForcesCollisionSingleGPU, N padded to {nr}, in its own units "
+                       f"(m_Si = 1), against the FP64 oracle in the same units")
         out["reference_kernel"] = res
     print(json.dumps(out))
     return out
@@ -792,7 +980,10 @@ def run_ours(a):
     import oracle as orc
 
     ctx = gi.Context(local, dense_min=a.dense_min)
-    pos, vel, nfe = make_workload(gi, torch, wl, 2 + rank, a.settle_steps)
+    state = load_state()
+    if state is None:  # the committed state is missing: settle it here
+        state = make_workload(gi, torch, wl, 2, a.settle_steps)
+    pos, vel, nfe = state
     n = len(pos)
     p = wl.params(gi)
     run = wl.run_desc(gi, 0, n, nfe)
@@ -801,8 +992,10 @@ def run_ours(a):
             (torch.empty((n, 4), dtype=torch.float32, device="cuda"),
              torch.empty((n, 4), dtype=torch.float32, device="cuda"))]
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > L2
-    stream = torch.cuda.current_stream()
+    # a stream of its own for the timed steps, their events and the flushes
+    stream = torch.cuda.Stream()
     s = stream.cuda_stream
+    torch.cuda.synchronize()  # the state copies above are complete
 
     def one_step(k):
         (pa, va), (pb, vb) = bufs[k % 2], bufs[(k + 1) % 2]
@@ -828,11 +1021,12 @@ def run_ours(a):
            for _ in range(a.steps)]
     t_wall = time.perf_counter()
     torch.cuda.nvtx.range_push("timed")  # lets ncu capture only the timed steps
-    for k in range(a.steps):
-        flush.fill_(float(k))
-        evs[k][0].record(stream)
-        one_step(nw + k)
-        evs[k][1].record(stream)
+    with torch.cuda.stream(stream):
+        for k in range(a.steps):
+            flush.fill_(float(k))
+            evs[k][0].record(stream)
+            one_step(nw + k)
+            evs[k][1].record(stream)
     torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     if world > 1:
@@ -889,7 +1083,16 @@ def run_ours(a):
         refgpu = None
         if not a.no_ref_gpu:
             refgpu = ref_gpu_baseline(gi, orc, torch, pos, vel, nfe, p)
+        accuracy = None if a.no_accuracy else accuracy_section(
+            gi, orc, torch, pos, vel, nfe, p, "settled config-2 state, step 0 of the timed steps")
         collision = None if a.no_collision else collision_section(torch, ctx, flush, dp, dv, run, p, a)
+        cstate = collision.pop("_state") if collision is not None else None
+        if cstate is not None and not a.no_accuracy:
+            cp, cv = cstate
+            collision["accuracy"] = accuracy_section(
+                gi, orc, torch, cp, cv, nfe, p,
+                f"collision phase: the timed state {a.collision_advance} steps later")
+        hbm = None if a.no_hbm else hbm_section(gi, torch, wl, ctx, pos, vel, nfe, p)
         large = None if a.no_large else large_n_section(gi, torch, wl, ctx, peak_sustained, a)
         sweep = None if a.no_sweep else sweep_section(gi, torch, wl, a)
         serve = None if a.no_serve else serve_section(gi, torch, wl, a)
@@ -897,17 +1100,15 @@ def run_ours(a):
             "metric": "interactions/s", "value": value, "unit": "interactions/s", "n_gpus": world,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded, settled on the GPU)",
-            "config": {"workload": "plain two-body impact: 60,000-body target + 6,000-body impactor, "
-                                   "30% Fe, spin 0.5 breakup, 45 deg, 1.2 v_esc, dt 1e-3",
-                       "n_bodies": n, "interactions_per_step": inter,
-                       "advance_steps": a.advance,
-                       "accumulation": "kahan (FP32 tiles of 128, compensated across tiles)",
-                       "tuning": {"i_per_thread": ipt, "jchunk": jchunk, "autotune_s": round(t_tune, 2)},
-                       "l2": "flushed between timed steps (256 MB write, outside the events)",
-                       "parallelism": f"replicas x{world}"},
+            "data": "synthetic (seeded, settled; bench_state/impact66k_seed2.npz)",
+            "config": bench_config(n, world, a.advance),
+            "impl": {"accumulation": "kahan (FP32 tiles of 128, compensated across tiles)",
+                     "tuning": {"i_per_thread": ipt, "jchunk": jchunk,
+                                "autotune_s": round(t_tune, 2)}},
             "fp32_tflops": achieved, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
-            "ref_gpu": refgpu, "collision_phase": collision, "large_n": large, "sweep": sweep, "serve": serve, "clocks": clk, "gpu_launches": 14 * a.steps,
+            "ref_gpu": refgpu, "accuracy": accuracy, "collision_phase": collision,
+            "hbm": hbm, "large_n": large, "sweep": sweep,
+            "serve": serve, "clocks": clk, "gpu_launches": 14 * a.steps,
             "wall_s_timed_region": t_wall, "state_finite": state_ok,
             "step_ms_min_max": [min(step_ms), max(step_ms)],
         }
@@ -919,31 +1120,31 @@ def run_ours(a):
 
 
 def run_reference(a):
-    """Reference arm: the reference's force/move loop on the host cores."""
+    """Reference arm: the reference's force loop (getForcesCollisionSingleGPU,
+    impactAddTime.cu:245-377, restated reference-exact in the oracle: the
+    reference has no host implementation of its own) on the host cores, on
+    the same settled state as the GPU arm.  Loads only the oracle's host
+    library: no GPU library is touched."""
     import numpy as np
     rank, local, world = dist_setup("gloo")
     if rank != 0:
         return None
     import oracle as orc
-    gi = _load("gi", os.path.join(PKG, "gi.py"))
-    wl = _load("gi_workloads", os.path.join(PKG, "gi_workloads.py"))
+    wl = _load("gi_workloads", os.path.join(PKG, "gi_workloads.py"))  # plain Python, no library
     b = _load("gi_build", os.path.join(PKG, "gi_build.py"))
     b.build_oracle()
-    p = wl.params(gi)
-    try:
-        import torch
-        if not torch.cuda.is_available():
-            raise RuntimeError("no GPU for input preparation")
-        pos, vel, nfe = make_workload(gi, torch, wl, 2, a.settle_steps)
-        prep = "state prepared (settled) on the GPU, then copied to the host"
-    except Exception as e:  # input preparation only; the timed loop is pure host code
-        pt, vt, fet = wl.raw_body(gi, 2, N_TARGET, 0.0, 1.0)
-        pi, vi, fei = wl.raw_body(gi, 1002, N_IMPACTOR, 2.0, 3.0)
-        pos, vel, nfe = wl.spin_and_place(np.concatenate([pt, pi]), np.concatenate([vt, vi]),
-                                          N_TARGET, N_IMPACTOR, fet, fei)
-        prep = f"unsettled bodies ({e})"
+    m = wl.MATERIAL
+    p = orc.material_params(m["G"], m["diameter"], m["mass_fe"], m["mass_si"], m["k_fe"],
+                            m["k_si"], m["kr_fe"], m["kr_si"], m["sd_fe"], m["sd_si"])
+    state = load_state()
+    if state is None:
+        line = {"impl": "reference", "unavailable": f"{STATE_FILE} missing (run "
+                                                     "bench_state/make_state.py)"}
+        print(json.dumps(line))
+        return line
+    pos, vel, nfe = state
     n = len(pos)
-    run = [(0, n, nfe, 0, wl.DT, wl.DT / 1.0, wl.DT / 0.4, 0.0)]
+    run = [(0, n, nfe, 0, wl.DT, wl.DT / m["mass_fe"], wl.DT / m["mass_si"], 0.0)]
     rng = np.random.default_rng(1)
     # size one step's i-sample so that warm-up + steps stay within ~3 minutes
     k = 256
@@ -967,9 +1168,8 @@ def run_reference(a):
     line = {"impl": "reference", "metric": "interactions/s", "value": value, "unit": "interactions/s",
             "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": full_step_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded)",
-            "config": {"workload": "plain two-body impact: 60,000 + 6,000 bodies (66,000)",
-                       "n_bodies": n, "input": prep},
+            "data": "synthetic (seeded, settled; bench_state/impact66k_seed2.npz)",
+            "config": bench_config(n, world, 0),
             "cpu_baseline": {"value": value, "unit": "interactions/s", "cores": orc.max_threads(),
                              "kind": "port",
                              "sample": f"per step {k} seeded i-bodies x all {n} j-bodies "
