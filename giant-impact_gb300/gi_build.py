@@ -6,6 +6,7 @@ Everything is compiled in-tree:
   oracle/libgi_oracle.so               CPU oracle (test infrastructure)
   oracle/_ref/libgiref.so              the reference's own kernels, extracted
                                        from its sources (test infrastructure)
+  oracle/_ref/libgirefhost.so          the reference's own host steps, likewise
 """
 from __future__ import annotations
 
@@ -118,12 +119,25 @@ def build_ref(force: bool = False) -> str | None:
     return build_ref.build(nvcc(), ARCH, force=force)
 
 
+def build_ref_host(force: bool = False) -> str | None:
+    """The reference's own host steps, cut from its sources and compiled for
+    the CPU (test infrastructure); None where no cut is available."""
+    sys.path.insert(0, ORACLE)
+    try:
+        import build_ref  # oracle/build_ref.py
+    finally:
+        sys.path.pop(0)
+    return build_ref.build_host(force=force)
+
+
 def build_all(force: bool = False) -> dict:
-    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+    with cf.ThreadPoolExecutor(max_workers=4) as ex:
         f_gi = ex.submit(build_libgi, force)
         f_or = ex.submit(build_oracle, force)
         f_ref = ex.submit(build_ref, force)
-        return {"libgi": f_gi.result(), "oracle": f_or.result(), "ref": f_ref.result()}
+        f_host = ex.submit(build_ref_host, force)
+        return {"libgi": f_gi.result(), "oracle": f_or.result(), "ref": f_ref.result(),
+                "ref_host": f_host.result()}
 
 
 if __name__ == "__main__":

@@ -11,7 +11,18 @@ by line range:
 into oracle/_ref/*.inc (git-ignored; never committed), and compiled together
 with oracle/ref_launch.cu (extern "C" launchers written for this project)
 for sm_103a with the reference's optimisation level (-O3, no fast math)
-into oracle/_ref/libgiref.so.  Each cut is checked against the lines it must
+into oracle/_ref/libgiref.so.
+
+The reference's host steps of building and setting up an impact are cut the
+same way and compiled for the CPU with oracle/ref_host.cpp (the globals and
+vector types they use, and extern "C" entry points) into
+oracle/_ref/libgirefhost.so:
+
+  Code/GenerateTargetImpactorCode/generateTargetImpactorBasicFunctions.h
+      29-237 (centre of mass, radius, mean velocity, angular momentum),
+      407-506 (spinBody, zeroOutTargetImpactorDrift)
+  Code/ImpactCode/impactInitialization.cu
+      183-391 (readImpactSetupParameters, setupInitialConditions)  Each cut is checked against the lines it must
 start and end with, so a moved line range fails loudly instead of compiling
 the wrong code.  Where the reference is absent (the GPU host), the cuts made
 earlier are compiled as they are.
@@ -50,11 +61,23 @@ CUTS = [
 ]
 
 
+HOST_CUTS = [
+    ("Code/GenerateTargetImpactorCode/generateTargetImpactorBasicFunctions.h", 29, 237,
+     {29: "double4 getCenterOfMass(int scope)"}, "ref_generate_getters.inc"),
+    ("Code/GenerateTargetImpactorCode/generateTargetImpactorBasicFunctions.h", 407, 506,
+     {407: "void spinBody(int bodyId, float4 spinVector)", 472: "void zeroOutTargetImpactorDrift()"},
+     "ref_generate_spin_drift.inc"),
+    ("Code/ImpactCode/impactInitialization.cu", 183, 391,
+     {183: "void readImpactSetupParameters()", 260: "void setupInitialConditions()"},
+     "ref_impact_setup.inc"),
+]
+
+
 def extract() -> bool:
     if not os.path.isdir(REFERENCE):
         return False
     os.makedirs(OUT, exist_ok=True)
-    for rel, a, b, expect, out in CUTS:
+    for rel, a, b, expect, out in CUTS + HOST_CUTS:
         with open(os.path.join(REFERENCE, rel), encoding="latin-1") as f:
             lines = f.read().split("\n")
         for ln, text in expect.items():
@@ -86,6 +109,29 @@ def build(nvcc: str, arch: list[str], force: bool = False) -> str | None:
         f.write(" ".join(cmd) + "\n" + p.stdout)
     if p.returncode != 0:
         raise RuntimeError("reference kernel build failed:\n" + p.stdout[-4000:])
+    return lib
+
+
+def build_host(force: bool = False) -> str | None:
+    """The reference's host steps (HOST_CUTS) with oracle/ref_host.cpp, for the
+    CPU, without FMA contraction (the reference's host code is compiled for
+    x86-64, where it has none)."""
+    extract()
+    incs = [os.path.join(OUT, c[4]) for c in HOST_CUTS]
+    if not all(os.path.exists(p) for p in incs):
+        return None
+    src = os.path.join(HERE, "ref_host.cpp")
+    lib = os.path.join(OUT, "libgirefhost.so")
+    deps = incs + [src]
+    if not force and os.path.exists(lib) and all(os.path.getmtime(d) <= os.path.getmtime(lib) for d in deps):
+        return lib
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-w", "-I", OUT,
+           src, "-o", lib]
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    with open(os.path.join(OUT, "build_host.log"), "w") as f:
+        f.write(" ".join(cmd) + "\n" + p.stdout)
+    if p.returncode != 0:
+        raise RuntimeError("reference host build failed:\n" + p.stdout[-4000:])
     return lib
 
 

@@ -246,6 +246,27 @@ def ref_lib():
     return _ref
 
 
+REF_HOST_LIB = os.path.join(HERE, "_ref", "libgirefhost.so")
+_ref_host = None
+
+
+def ref_host_lib():
+    """The reference's own host steps (oracle/_ref/libgirefhost.so, cut from
+    its sources), or None."""
+    global _ref_host
+    if _ref_host is None and os.path.exists(REF_HOST_LIB):
+        L = C.CDLL(REF_HOST_LIB)
+        P, I, D = C.c_void_p, C.c_int, C.c_double
+        L.giref_host_spin.argtypes = [P, P, P, D, D, D, D, I, P]
+        L.giref_host_spin.restype = None
+        L.giref_host_zero_drift.argtypes = [P, P, P, D, D, D, D]
+        L.giref_host_zero_drift.restype = None
+        L.giref_host_impact_setup.argtypes = [C.c_char_p, P, D, D, P, P]
+        L.giref_host_impact_setup.restype = I
+        _ref_host = L
+    return _ref_host
+
+
 def groups_ref(pos, touch=1.5):
     """Group number of every body, the reference's literal O(N^2) loop."""
     pos = _f32(pos)

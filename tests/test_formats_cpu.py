@@ -16,6 +16,7 @@ import pytest
 
 import build_ref
 import formats_oracle as fo
+from oracle import ref_host_lib as orc_ref_host
 from conftest import ROOT
 
 # The reference's Code/ folder (GI_REFERENCE_DIR, see oracle/build_ref.py);
@@ -385,6 +386,73 @@ def test_impact_initial_conditions_and_stats(gi, tmp_path):
     st = gi.system_stats_host(P, V, nfe, b.mass_fe, b.mass_si)
     want = fo.system_stats(P, V, nfe, b.mass_fe, b.mass_si)
     assert st == want
+
+
+# ------------------------------------ host steps vs the reference's own code --
+
+needs_ref_host = pytest.mark.skipif(
+    orc_ref_host() is None, reason="the reference's host steps are not built (no cut available)")
+
+
+@needs_ref_host
+def test_spin_and_drift_bitwise_vs_reference_code(gi, tmp_path):
+    """gi_spin_body and gi_zero_drift against the reference's own spinBody and
+    zeroOutTargetImpactorDrift (generateTargetImpactorBasicFunctions.h:
+    407-506), compiled from its sources, on the same bodies: every bit."""
+    import ctypes as C
+    ref = orc_ref_host()
+    setup, plan = _plan(gi, tmp_path)
+    b = plan.body
+    counts = (C.c_int * 4)(b.nfe1, b.nsi1, b.nfe2, b.nsi2)
+    for seed in (41, 42):
+        pos, vel, _ = gi.raw_bodies(seed, b)
+        rng = np.random.default_rng(seed)
+        vel[:, :3] = rng.normal(scale=0.05, size=(len(vel), 3)).astype(np.float32)
+        mp, mv = pos.copy(), vel.copy()
+        rp, rv = pos.copy(), vel.copy()
+        for body, axis, w in ((1, list(setup.spin1[:3]), plan.spin1_w),
+                              (2, list(setup.spin2[:3]), plan.spin2_w),
+                              (1, [0.3, -2.0, 0.5], 0.125)):
+            gi.spin_body(mp, mv, plan, body, axis, w)
+            spin = (C.c_float * 4)(*axis, w)
+            ref.giref_host_spin(rp.ctypes.data, rv.ctypes.data, counts, b.mass_fe, b.mass_si,
+                                plan.mass_body1, plan.mass_body2, body, spin)
+            assert np.array_equal(mv, rv), (seed, body)
+        gi.zero_drift(mp, mv, plan)
+        ref.giref_host_zero_drift(rp.ctypes.data, rv.ctypes.data, counts, b.mass_fe, b.mass_si,
+                                  plan.mass_body1, plan.mass_body2)
+        assert np.array_equal(mp, rp) and np.array_equal(mv, rv)
+
+
+@needs_ref_host
+def test_impact_initial_conditions_bitwise_vs_reference_code(gi, tmp_path):
+    """gi_impact_initial_conditions against the reference's own
+    readImpactSetupParameters + setupInitialConditions
+    (impactInitialization.cu:183-391), compiled from its sources and run in
+    a folder laid out as its drivers expect: the same initial frame, bit for
+    bit (unit conversion in float, offsets added, [Fe1, Fe2, Si1, Si2])."""
+    import ctypes as C
+    ref = orc_ref_host()
+    _, plan = _plan(gi, tmp_path)
+    b = plan.body
+    pos, vel, _ = gi.raw_bodies(43, b)
+    rng = np.random.default_rng(43)
+    vel[:, :3] = rng.normal(scale=0.02, size=(len(vel), 3)).astype(np.float32)
+    root = tmp_path / "run"
+    (root / "TargetImpactorInformation").mkdir(parents=True)
+    work = root / "a" / "b"
+    work.mkdir(parents=True)
+    gi.write_body_file(str(root / "TargetImpactorInformation" / "targetImpactorInitialPosVel"),
+                       pos, vel)
+    (root / "setupImpactInitialization").write_text(SETUP_IMPACT_INIT)
+    s = gi.read_setup_impact_init(str(root / "setupImpactInitialization"))
+    P, V = gi.impact_initial_conditions(b, s, pos, vel)
+    RP = np.zeros_like(P)
+    RV = np.zeros_like(V)
+    counts = (C.c_int * 4)(b.nfe1, b.nsi1, b.nfe2, b.nsi2)
+    assert ref.giref_host_impact_setup(str(work).encode(), counts, b.unit_length, b.unit_time,
+                                       RP.ctypes.data, RV.ctypes.data) == 0
+    assert np.array_equal(P, RP) and np.array_equal(V, RV)
 
 
 # ------------------------------------------------- writers vs the sources --
