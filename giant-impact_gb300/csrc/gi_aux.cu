@@ -44,16 +44,98 @@ __device__ __forceinline__ bool in_scope(const unsigned char *label, int i, int 
     return l == 3;
 }
 
+// The sums of the diagnostics are kept per thread in float-float pairs on
+// the FP32 pipe: a value is hi + lo, about 48 significant bits.  TwoSum and
+// the FMA form of TwoProd are error-free, and every addition renormalises
+// the pair, so a thread's sum of n terms is exact to about n 2^-48 of the
+// terms' magnitudes.  This GPU issues FP64 at a small fraction of its FP32
+// rate: with the per-body work in FP64 the two passes ran at ~850 GB/s, with
+// it on the FP32 pipe they are bound by HBM.  FP64 remains for the block
+// partials and everything after them.
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// a += xh + xl, renormalised (|lo| <= ulp(hi) / 2).
+__device__ __forceinline__ void ff_add2(FF &a, float xh, float xl)
+{
+    float s, e;
+    two_sum(a.hi, xh, s, e);
+    e = __fadd_rn(e, __fadd_rn(a.lo, xl));
+    a.hi = __fadd_rn(s, e);
+    a.lo = __fsub_rn(e, __fsub_rn(a.hi, s));
+}
+
+__device__ __forceinline__ void ff_add(FF &a, float x) { ff_add2(a, x, 0.0f); }
+
+// a += x * y, the product taken exactly (p + e with e = fma(x, y, -p)).
+__device__ __forceinline__ void ff_add_prod(FF &a, float x, float y)
+{
+    const float p = __fmul_rn(x, y);
+    ff_add2(a, p, __fmaf_rn(x, y, -p));
+}
+
+// x - c for a float x and a double c given as ch + cl (ch = (float)c):
+// TwoSum of x and -ch is exact, cl is folded into the low part.
+__device__ __forceinline__ FF ff_sub_d(float x, float ch, float cl)
+{
+    FF r;
+    float e;
+    two_sum(x, -ch, r.hi, e);
+    r.lo = __fsub_rn(e, cl);
+    return r;
+}
+
+// a += u v - w z for float-float u, v, w, z: each product's high part
+// exact, its cross terms to 2^-24 of themselves, the lo * lo terms
+// (2^-48 of the product) left out.
+__device__ __forceinline__ void ff_add_cross(FF &a, FF u, FF v, FF w, FF z)
+{
+    const float p1 = __fmul_rn(u.hi, v.hi);
+    float e1 = __fmaf_rn(u.hi, v.hi, -p1);
+    e1 = __fmaf_rn(u.hi, v.lo, __fmaf_rn(u.lo, v.hi, e1));
+    const float p2 = __fmul_rn(w.hi, z.hi);
+    float e2 = __fmaf_rn(w.hi, z.hi, -p2);
+    e2 = __fmaf_rn(w.hi, z.lo, __fmaf_rn(w.lo, z.hi, e2));
+    float s, t;
+    two_sum(p1, -p2, s, t);
+    ff_add2(a, s, __fadd_rn(t, __fsub_rn(e1, e2)));
+}
+
+__device__ __forceinline__ double ff_value(const FF &a) { return (double)a.hi + (double)a.lo; }
+
+// Sum of the lanes' pairs to lane 0 (float-float), NV of them.
 template <int NV>
-__device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *dst)
+__device__ __forceinline__ void warp_ff_sum(FF (&v)[NV])
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            const float h = __shfl_down_sync(0xffffffffu, v[c].hi, o);
+            const float l = __shfl_down_sync(0xffffffffu, v[c].lo, o);
+            ff_add2(v[c], h, l);
+        }
+    }
+}
+
+// Lane 0 of each warp passes its values (FP64); the block's warps are
+// added in warp order and thread c < NV writes value c of the block.
+template <int NV>
+__device__ __forceinline__ void block_store(const double (&v)[NV], double *dst)
 {
     __shared__ double sh[NV][8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
 #pragma unroll
-    for (int c = 0; c < NV; ++c) {
-        double x = v[c];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sh[c][warp] = x;
+        for (int c = 0; c < NV; ++c) sh[c][warp] = v[c];
     }
     __syncthreads();
     if (threadIdx.x < NV) {
@@ -64,77 +146,136 @@ __device__ __forceinline__ void block_reduce_store(double (&v)[NV], double *dst)
     }
 }
 
+// Both passes give each block one material class: blockIdx.y = 0 takes the
+// run's Fe bodies [0, nfe), 1 its Si bodies [nfe, n), in a grid-stride
+// loop over blockIdx.x, so the class mass multiplies the block's sums once,
+// in FP64.  Block b's partials are work[16 b ..], b = y gridDim.x + x.
+
 // Pass 1: mass, sum m x, sum m v, kinetic energy, count (9 doubles / block).
 __global__ void __launch_bounds__(256)
 diag_pass1(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
            const unsigned char *__restrict__ label, int scope, int off, int n,
            int nfe, double mfe, double msi, double *__restrict__ work)
 {
-    double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int k0 = blockIdx.y == 0 ? 0 : nfe, k1 = blockIdx.y == 0 ? nfe : n;
+    const double m = blockIdx.y == 0 ? mfe : msi;
+    FF v[7];
+#pragma unroll
+    for (int c = 0; c < 7; ++c) v[c] = FF{0.0f, 0.0f};
+    int cnt = 0;
+    for (int k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
         const int i = off + k;
         if (!in_scope(label, i, scope)) continue;
-        const double m = (k < nfe) ? mfe : msi;
         const float4 p = pos[i], u = vel[i];
-        v[0] += m;
-        v[1] += m * p.x; v[2] += m * p.y; v[3] += m * p.z;
-        v[4] += m * u.x; v[5] += m * u.y; v[6] += m * u.z;
-        v[7] += 0.5 * m * ((double)u.x * u.x + (double)u.y * u.y + (double)u.z * u.z);
-        v[8] += 1.0;
+        ff_add(v[0], p.x);
+        ff_add(v[1], p.y);
+        ff_add(v[2], p.z);
+        ff_add(v[3], u.x);
+        ff_add(v[4], u.y);
+        ff_add(v[5], u.z);
+        ff_add_prod(v[6], u.x, u.x);
+        ff_add_prod(v[6], u.y, u.y);
+        ff_add_prod(v[6], u.z, u.z);
+        ++cnt;
     }
-    block_reduce_store<9>(v, work + 16 * blockIdx.x);
+    warp_ff_sum<7>(v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    const double d[9] = {m * cnt,
+                         m * ff_value(v[0]), m * ff_value(v[1]), m * ff_value(v[2]),
+                         m * ff_value(v[3]), m * ff_value(v[4]), m * ff_value(v[5]),
+                         0.5 * m * ff_value(v[6]), (double)cnt};
+    block_store<9>(d, work + 16 * (blockIdx.y * gridDim.x + blockIdx.x));
 }
 
-// Finalise pass 1 in block order; out = [mass, com3, vcom3, -, -, -, ke, p3, count].
-__global__ void diag_fin1(const double *__restrict__ work, int nblocks, double *out)
+// Block partials summed in a fixed order (thread t takes blocks t, t + 256,
+// ..., then a tree over the threads): deterministic.  Run as one block of
+// 256 threads; the sums end in sh[c][0].
+template <int NV>
+__device__ __forceinline__ void ordered_sums(const double *__restrict__ work, int nblocks,
+                                             double (&sh)[NV][256])
 {
+    const int t = threadIdx.x;
+    double v[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) v[c] = 0.0;
+    for (int b = t; b < nblocks; b += 256)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) v[c] += work[16 * b + c];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) sh[c][t] = v[c];
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (t < s)
+#pragma unroll
+            for (int c = 0; c < NV; ++c) sh[c][t] += sh[c][t + s];
+        __syncthreads();
+    }
+}
+
+// Finalise pass 1; out = [mass, com3, vcom3, -, -, -, ke, p3, count].
+__global__ void __launch_bounds__(256) diag_fin1(const double *__restrict__ work, int nblocks,
+                                                 double *out)
+{
+    __shared__ double sh[9][256];
+    ordered_sums<9>(work, nblocks, sh);
     if (threadIdx.x != 0) return;
-    double t[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int b = 0; b < nblocks; ++b)
-        for (int c = 0; c < 9; ++c) t[c] += work[16 * b + c];
-    const double m = t[0];
+    const double m = sh[0][0];
     out[0] = m;
     for (int c = 0; c < 3; ++c) {
-        out[1 + c] = m > 0.0 ? t[1 + c] / m : 0.0;
-        out[4 + c] = m > 0.0 ? t[4 + c] / m : 0.0;
-        out[11 + c] = t[4 + c];
+        out[1 + c] = m > 0.0 ? sh[1 + c][0] / m : 0.0;
+        out[4 + c] = m > 0.0 ? sh[4 + c][0] / m : 0.0;
+        out[11 + c] = sh[4 + c][0];
     }
-    out[10] = t[7];
-    out[14] = t[8];
+    out[10] = sh[7][0];
+    out[14] = sh[8][0];
 }
 
 // Pass 2: angular momentum about the com, relative to the com velocity
-// (impactBasicFunctions.h:507-652 in double).
+// (impactBasicFunctions.h:507-652 in double): r = x - com and w = v - vcom
+// as float-float pairs, sum of r x w per class.
 __global__ void __launch_bounds__(256)
 diag_pass2(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
            const unsigned char *__restrict__ label, int scope, int off, int n,
            int nfe, double mfe, double msi, const double *__restrict__ out,
            double *__restrict__ work)
 {
-    const double cx = out[1], cy = out[2], cz = out[3];
-    const double ux = out[4], uy = out[5], uz = out[6];
-    double v[3] = {0, 0, 0};
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int k0 = blockIdx.y == 0 ? 0 : nfe, k1 = blockIdx.y == 0 ? nfe : n;
+    const double m = blockIdx.y == 0 ? mfe : msi;
+    float ch[6], cl[6];  // com xyz, vcom xyz as float pairs
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const double x = out[1 + c];
+        ch[c] = (float)x;
+        cl[c] = (float)(x - (double)ch[c]);
+    }
+    FF L[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) L[c] = FF{0.0f, 0.0f};
+    for (int k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
         const int i = off + k;
         if (!in_scope(label, i, scope)) continue;
-        const double m = (k < nfe) ? mfe : msi;
         const float4 p = pos[i], u = vel[i];
-        const double rx = p.x - cx, ry = p.y - cy, rz = p.z - cz;
-        const double wx = u.x - ux, wy = u.y - uy, wz = u.z - uz;
-        v[0] += (ry * wz - rz * wy) * m;
-        v[1] += -(rx * wz - rz * wx) * m;
-        v[2] += (rx * wy - ry * wx) * m;
+        const FF rx = ff_sub_d(p.x, ch[0], cl[0]), ry = ff_sub_d(p.y, ch[1], cl[1]),
+                 rz = ff_sub_d(p.z, ch[2], cl[2]);
+        const FF wx = ff_sub_d(u.x, ch[3], cl[3]), wy = ff_sub_d(u.y, ch[4], cl[4]),
+                 wz = ff_sub_d(u.z, ch[5], cl[5]);
+        ff_add_cross(L[0], ry, wz, rz, wy);
+        ff_add_cross(L[1], rz, wx, rx, wz);
+        ff_add_cross(L[2], rx, wy, ry, wx);
     }
-    block_reduce_store<3>(v, work + 16 * blockIdx.x);
+    warp_ff_sum<3>(L);
+    const double d[3] = {m * ff_value(L[0]), m * ff_value(L[1]), m * ff_value(L[2])};
+    block_store<3>(d, work + 16 * (blockIdx.y * gridDim.x + blockIdx.x));
 }
 
-__global__ void diag_fin2(const double *__restrict__ work, int nblocks, double *out)
+__global__ void __launch_bounds__(256) diag_fin2(const double *__restrict__ work, int nblocks,
+                                                 double *out)
 {
+    __shared__ double sh[3][256];
+    ordered_sums<3>(work, nblocks, sh);
     if (threadIdx.x != 0) return;
-    double t[3] = {0, 0, 0};
-    for (int b = 0; b < nblocks; ++b)
-        for (int c = 0; c < 3; ++c) t[c] += work[16 * b + c];
-    out[7] = t[0]; out[8] = t[1]; out[9] = t[2];
+    out[7] = sh[0][0]; out[8] = sh[1][0]; out[9] = sh[2][0];
 }
 
 // -------------------------------------------------------------- potential --
@@ -248,12 +389,14 @@ cudaError_t gi_launch_diag(const float4 *pos, const float4 *vel,
                            cudaStream_t s)
 {
     (void)par;
-    gi::diag_pass1<<<nblocks, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n,
-                                           run.nfe, mass_fe, mass_si, work);
-    gi::diag_fin1<<<1, 32, 0, s>>>(work, nblocks, out_dev);
-    gi::diag_pass2<<<nblocks, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n,
-                                           run.nfe, mass_fe, mass_si, out_dev, work);
-    gi::diag_fin2<<<1, 32, 0, s>>>(work, nblocks, out_dev);
+    // blockIdx.y: the run's Fe bodies, then its Si bodies
+    const dim3 grid((unsigned)(nblocks / 2), 2);
+    gi::diag_pass1<<<grid, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
+                                        mass_fe, mass_si, work);
+    gi::diag_fin1<<<1, 256, 0, s>>>(work, 2 * (nblocks / 2), out_dev);
+    gi::diag_pass2<<<grid, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
+                                        mass_fe, mass_si, out_dev, work);
+    gi::diag_fin2<<<1, 256, 0, s>>>(work, 2 * (nblocks / 2), out_dev);
     return cudaGetLastError();
 }
 

@@ -424,6 +424,50 @@ def test_diag_and_potential_vs_oracle(gi, orc, torch_cuda, ctx):
     assert u == pytest.approx(u64, rel=1e-7)
 
 
+def test_diag_far_from_origin_and_moving(gi, orc, torch_cuda, ctx):
+    """The FP64 diagnostics keep their per-body sums in float-float pairs on
+    the FP32 pipe.  Here 300,000 bodies sit 1.1e4 D from the origin, move at
+    a bulk 32 D per time unit and spin slowly, so the angular momentum about
+    the centre of mass is far smaller than the orbital term M c x u, and the
+    centre of mass is a small difference of large sums.  Against the FP64
+    oracle (sequential double sums): every quantity to about 1e-12 of its
+    own scale, the angular momentum to 1e-10 of sum |m r x w|."""
+    torch = torch_cuda
+    n = 300000
+    rng = np.random.default_rng(21)
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    r = 30.0 * rng.uniform(0, 1, size=(n, 1)) ** (1 / 3)
+    x = d * r
+    w = 0.01 * np.stack([-x[:, 1], x[:, 0], np.zeros(n)], 1)  # spin about z
+    pos = np.zeros((n, 4), np.float32)
+    vel = np.zeros((n, 4), np.float32)
+    pos[:, :3] = x + np.array([1.0e4, -5.0e3, 2.0e3])
+    vel[:, :3] = w + rng.normal(scale=0.5, size=(n, 3)) + np.array([30.0, -10.0, 5.0])
+    nfe = n // 10
+    p = config1_params(gi)
+    run = gi.Run(0, n, nfe, 0, 0, 0, 0, 0)
+    dp, dv = dev(torch, pos), dev(torch, vel)
+    got = np.array(ctx.diag(dp.data_ptr(), dv.data_ptr(), run, p))
+    want = orc.diag_fp64(pos, vel, (0, n, nfe, 0, 0, 0, 0, 0), p)
+    m = np.where(np.arange(n) < nfe, p.MassFe, p.MassSi).astype(np.float64)
+    P64, V64 = pos[:, :3].astype(np.float64), vel[:, :3].astype(np.float64)
+    assert got[14] == want[14] == n
+    assert abs(got[0] - want[0]) <= 1e-13 * want[0]
+    assert np.abs(got[1:4] - want[1:4]).max() <= 1e-12 * np.abs(P64).max()
+    assert np.abs(got[4:7] - want[4:7]).max() <= 1e-12 * np.abs(V64).max()
+    assert abs(got[10] - want[10]) <= 1e-12 * want[10]
+    assert np.abs(got[11:14] - want[11:14]).max() <= 1e-12 * (m[:, None] * np.abs(V64)).sum()
+    rr, ww = P64 - want[1:4], V64 - want[4:7]
+    scale = (m[:, None] * np.abs(np.cross(rr, ww))).sum()
+    err = np.abs(got[7:10] - want[7:10]).max()
+    print(f"L about the com {want[7:10]}, |error| {err:.3e}, sum |m r x w| {scale:.3e}")
+    assert err <= 1e-10 * scale
+    # the same call twice gives the same bits
+    again = np.array(ctx.diag(dp.data_ptr(), dv.data_ptr(), run, p))
+    assert np.array_equal(got, again)
+
+
 def test_run_host_matches_device_path(gi, torch_cuda, ctx):
     torch = torch_cuda
     import gi_workloads as wl
