@@ -292,7 +292,7 @@ static int ctx_init(gi_ctx *c, int device)
         return fail(GI_ERR_NO_DEVICE, "libgi is built for sm_103 only; device %d is sm_%d%d",
                     device, prop.major, prop.minor);
     c->sm_count = prop.multiProcessorCount;
-    c->diag_blocks = 8 * c->sm_count;  // 4 per SM for each material class
+    c->diag_blocks = 16 * c->sm_count;  // shared by the two material classes
     DeviceGuard g(device);
     for (int acc = 0; acc < 3; ++acc)
         for (int p : {1, 2, 4, 8}) {

@@ -146,24 +146,36 @@ __device__ __forceinline__ void block_store(const double (&v)[NV], double *dst)
     }
 }
 
-// Both passes give each block one material class: blockIdx.y = 0 takes the
-// run's Fe bodies [0, nfe), 1 its Si bodies [nfe, n), in a grid-stride
-// loop over blockIdx.x, so the class mass multiplies the block's sums once,
-// in FP64.  Block b's partials are work[16 b ..], b = y gridDim.x + x.
+// Both passes give each block one material class, so the class mass
+// multiplies the block's sums once, in FP64: blocks [0, nbfe) take the
+// run's Fe bodies [0, nfe), blocks [nbfe, gridDim.x) its Si bodies [nfe, n),
+// each class in a grid-stride loop over its own blocks (nbfe in proportion
+// to nfe).  Block b's partials are work[16 b ..].
+__device__ __forceinline__ void class_range(int nfe, int n, int nbfe, double mfe, double msi,
+                                            int &k0, int &k1, int &b, int &nb, double &m)
+{
+    const bool fe = (int)blockIdx.x < nbfe;
+    k0 = fe ? 0 : nfe;
+    k1 = fe ? nfe : n;
+    b = fe ? (int)blockIdx.x : (int)blockIdx.x - nbfe;
+    nb = fe ? nbfe : (int)gridDim.x - nbfe;
+    m = fe ? mfe : msi;
+}
 
 // Pass 1: mass, sum m x, sum m v, kinetic energy, count (9 doubles / block).
 __global__ void __launch_bounds__(256)
 diag_pass1(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
            const unsigned char *__restrict__ label, int scope, int off, int n,
-           int nfe, double mfe, double msi, double *__restrict__ work)
+           int nfe, int nbfe, double mfe, double msi, double *__restrict__ work)
 {
-    const int k0 = blockIdx.y == 0 ? 0 : nfe, k1 = blockIdx.y == 0 ? nfe : n;
-    const double m = blockIdx.y == 0 ? mfe : msi;
+    int k0, k1, b, nb;
+    double m;
+    class_range(nfe, n, nbfe, mfe, msi, k0, k1, b, nb, m);
     FF v[7];
 #pragma unroll
     for (int c = 0; c < 7; ++c) v[c] = FF{0.0f, 0.0f};
     int cnt = 0;
-    for (int k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+    for (int k = k0 + b * blockDim.x + threadIdx.x; k < k1; k += nb * blockDim.x) {
         const int i = off + k;
         if (!in_scope(label, i, scope)) continue;
         const float4 p = pos[i], u = vel[i];
@@ -185,7 +197,7 @@ diag_pass1(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                          m * ff_value(v[0]), m * ff_value(v[1]), m * ff_value(v[2]),
                          m * ff_value(v[3]), m * ff_value(v[4]), m * ff_value(v[5]),
                          0.5 * m * ff_value(v[6]), (double)cnt};
-    block_store<9>(d, work + 16 * (blockIdx.y * gridDim.x + blockIdx.x));
+    block_store<9>(d, work + 16 * blockIdx.x);
 }
 
 // Block partials summed in a fixed order (thread t takes blocks t, t + 256,
@@ -237,11 +249,12 @@ __global__ void __launch_bounds__(256) diag_fin1(const double *__restrict__ work
 __global__ void __launch_bounds__(256)
 diag_pass2(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
            const unsigned char *__restrict__ label, int scope, int off, int n,
-           int nfe, double mfe, double msi, const double *__restrict__ out,
+           int nfe, int nbfe, double mfe, double msi, const double *__restrict__ out,
            double *__restrict__ work)
 {
-    const int k0 = blockIdx.y == 0 ? 0 : nfe, k1 = blockIdx.y == 0 ? nfe : n;
-    const double m = blockIdx.y == 0 ? mfe : msi;
+    int k0, k1, b, nb;
+    double m;
+    class_range(nfe, n, nbfe, mfe, msi, k0, k1, b, nb, m);
     float ch[6], cl[6];  // com xyz, vcom xyz as float pairs
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -252,7 +265,7 @@ diag_pass2(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
     FF L[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) L[c] = FF{0.0f, 0.0f};
-    for (int k = k0 + blockIdx.x * blockDim.x + threadIdx.x; k < k1; k += gridDim.x * blockDim.x) {
+    for (int k = k0 + b * blockDim.x + threadIdx.x; k < k1; k += nb * blockDim.x) {
         const int i = off + k;
         if (!in_scope(label, i, scope)) continue;
         const float4 p = pos[i], u = vel[i];
@@ -266,7 +279,7 @@ diag_pass2(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
     }
     warp_ff_sum<3>(L);
     const double d[3] = {m * ff_value(L[0]), m * ff_value(L[1]), m * ff_value(L[2])};
-    block_store<3>(d, work + 16 * (blockIdx.y * gridDim.x + blockIdx.x));
+    block_store<3>(d, work + 16 * blockIdx.x);
 }
 
 __global__ void __launch_bounds__(256) diag_fin2(const double *__restrict__ work, int nblocks,
@@ -389,14 +402,18 @@ cudaError_t gi_launch_diag(const float4 *pos, const float4 *vel,
                            cudaStream_t s)
 {
     (void)par;
-    // blockIdx.y: the run's Fe bodies, then its Si bodies
-    const dim3 grid((unsigned)(nblocks / 2), 2);
-    gi::diag_pass1<<<grid, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
-                                        mass_fe, mass_si, work);
-    gi::diag_fin1<<<1, 256, 0, s>>>(work, 2 * (nblocks / 2), out_dev);
-    gi::diag_pass2<<<grid, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
-                                        mass_fe, mass_si, out_dev, work);
-    gi::diag_fin2<<<1, 256, 0, s>>>(work, 2 * (nblocks / 2), out_dev);
+    // blocks for the Fe bodies in proportion to their number (at least one
+    // when there are any), the rest for the Si bodies
+    if (nblocks < 2) return cudaErrorInvalidValue;
+    int nbfe = run.n > 0 ? (int)((long long)nblocks * run.nfe / run.n) : 0;
+    if (run.nfe > 0 && nbfe < 1) nbfe = 1;
+    if (nbfe > nblocks - 1) nbfe = nblocks - 1;
+    gi::diag_pass1<<<nblocks, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
+                                           nbfe, mass_fe, mass_si, work);
+    gi::diag_fin1<<<1, 256, 0, s>>>(work, nblocks, out_dev);
+    gi::diag_pass2<<<nblocks, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
+                                           nbfe, mass_fe, mass_si, out_dev, work);
+    gi::diag_fin2<<<1, 256, 0, s>>>(work, nblocks, out_dev);
     return cudaGetLastError();
 }
 
