@@ -175,10 +175,7 @@ diag_pass1(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
 #pragma unroll
     for (int c = 0; c < 7; ++c) v[c] = FF{0.0f, 0.0f};
     int cnt = 0;
-    for (int k = k0 + b * blockDim.x + threadIdx.x; k < k1; k += nb * blockDim.x) {
-        const int i = off + k;
-        if (!in_scope(label, i, scope)) continue;
-        const float4 p = pos[i], u = vel[i];
+    const auto body = [&](float4 p, float4 u) {
         ff_add(v[0], p.x);
         ff_add(v[1], p.y);
         ff_add(v[2], p.z);
@@ -189,7 +186,18 @@ diag_pass1(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
         ff_add_prod(v[6], u.y, u.y);
         ff_add_prod(v[6], u.z, u.z);
         ++cnt;
+    };
+    // two bodies' loads in flight at a time; each thread still takes its
+    // bodies in grid-stride order
+    const int stride = nb * blockDim.x;
+    int k = k0 + b * blockDim.x + threadIdx.x;
+    for (; k + stride < k1; k += 2 * stride) {
+        const int i0 = off + k, i1 = i0 + stride;
+        const float4 p0 = pos[i0], u0 = vel[i0], p1 = pos[i1], u1 = vel[i1];
+        if (in_scope(label, i0, scope)) body(p0, u0);
+        if (in_scope(label, i1, scope)) body(p1, u1);
     }
+    if (k < k1 && in_scope(label, off + k, scope)) body(pos[off + k], vel[off + k]);
     warp_ff_sum<7>(v);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
@@ -265,10 +273,7 @@ diag_pass2(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
     FF L[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) L[c] = FF{0.0f, 0.0f};
-    for (int k = k0 + b * blockDim.x + threadIdx.x; k < k1; k += nb * blockDim.x) {
-        const int i = off + k;
-        if (!in_scope(label, i, scope)) continue;
-        const float4 p = pos[i], u = vel[i];
+    const auto body = [&](float4 p, float4 u) {
         const FF rx = ff_sub_d(p.x, ch[0], cl[0]), ry = ff_sub_d(p.y, ch[1], cl[1]),
                  rz = ff_sub_d(p.z, ch[2], cl[2]);
         const FF wx = ff_sub_d(u.x, ch[3], cl[3]), wy = ff_sub_d(u.y, ch[4], cl[4]),
@@ -276,7 +281,16 @@ diag_pass2(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
         ff_add_cross(L[0], ry, wz, rz, wy);
         ff_add_cross(L[1], rz, wx, rx, wz);
         ff_add_cross(L[2], rx, wy, ry, wx);
+    };
+    const int stride = nb * blockDim.x;
+    int k = k0 + b * blockDim.x + threadIdx.x;
+    for (; k + stride < k1; k += 2 * stride) {
+        const int i0 = off + k, i1 = i0 + stride;
+        const float4 p0 = pos[i0], u0 = vel[i0], p1 = pos[i1], u1 = vel[i1];
+        if (in_scope(label, i0, scope)) body(p0, u0);
+        if (in_scope(label, i1, scope)) body(p1, u1);
     }
+    if (k < k1 && in_scope(label, off + k, scope)) body(pos[off + k], vel[off + k]);
     warp_ff_sum<3>(L);
     const double d[3] = {m * ff_value(L[0]), m * ff_value(L[1]), m * ff_value(L[2])};
     block_store<3>(d, work + 16 * blockIdx.x);
