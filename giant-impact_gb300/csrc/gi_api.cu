@@ -264,12 +264,13 @@ struct StreamScratch {
 struct gi_ctx {
     int device = 0;
     int sm_count = 0;
-    gi_options opt{GI_SEP_REF_INT, GI_ACCUM_KAHAN, 0, 0};
+    gi_options opt{GI_SEP_REF_INT, GI_ACCUM_PAIRED, 0, 0};
     bool forced = false;
     gi_tuning forced_tuning{0, 0};
     // Tuned i-bodies per thread per N bucket (floor(log2 n)); 0 = default.
     int bucket_ipt[32] = {0};
     int bucket_shift[32] = {0};  // big-chunk size scale 2^shift of the default
+    int bucket_pshift[32] = {0};  // GI_ACCUM_PAIRED: chunks per item scale 2^shift
     std::map<cudaStream_t, StreamScratch> scratch;
     float4 *mirror_pos = nullptr, *mirror_vel = nullptr;
     size_t mirror_cap = 0;
@@ -277,7 +278,7 @@ struct gi_ctx {
     int diag_blocks = 0;
     double *pot_buf = nullptr;
     size_t pot_cap = 0;
-    int occ[3][9];  // resident force CTAs per SM: [accum][i-bodies per thread]
+    int occ[4][9];  // resident one-sided force CTAs per SM: [accum][i-bodies per thread]
 };
 
 static int ctx_init(gi_ctx *c, int device)
@@ -294,7 +295,7 @@ static int ctx_init(gi_ctx *c, int device)
     c->sm_count = prop.multiProcessorCount;
     c->diag_blocks = 16 * c->sm_count;  // shared by the two material classes
     DeviceGuard g(device);
-    for (int acc = 0; acc < 3; ++acc)
+    for (int acc : {GI_ACC_KAHAN, GI_ACC_FP32, GI_ACC_FP64})
         for (int p : {1, 2, 4, 8}) {
             const int o = std::min({gi_force_occupancy(p, acc, GI_EPI_FORCE),
                                     gi_force_occupancy(p, acc, GI_EPI_STEP),
@@ -355,7 +356,7 @@ extern "C" int gi_ctx_set_options(gi_ctx *c, const gi_options *o)
     if (!c || !o) return fail(GI_ERR_INVALID_ARG, "NULL argument");
     if (o->sep_test != GI_SEP_REF_INT && o->sep_test != GI_SEP_SIGN)
         return fail(GI_ERR_INVALID_ARG, "sep_test %d", o->sep_test);
-    if (o->accum < GI_ACCUM_KAHAN || o->accum > GI_ACCUM_FP64)
+    if (o->accum < GI_ACCUM_PAIRED || o->accum > GI_ACCUM_KAHAN)
         return fail(GI_ERR_INVALID_ARG, "accum %d", o->accum);
     if (o->dense_min < 0) return fail(GI_ERR_INVALID_ARG, "dense_min %d", o->dense_min);
     if (o->cluster_tries < 0) return fail(GI_ERR_INVALID_ARG, "cluster_tries %d", o->cluster_tries);
@@ -370,10 +371,10 @@ extern "C" int gi_ctx_set_tuning(gi_ctx *c, const gi_tuning *t)
     if (t->i_per_thread != 1 && t->i_per_thread != 2 && t->i_per_thread != 4 &&
         t->i_per_thread != 8)
         return fail(GI_ERR_INVALID_ARG, "i_per_thread must be 1, 2, 4 or 8");
-    if (t->jchunk < 0 || t->jchunk % GI_NT != 0 ||
-        (t->jchunk > 0 && (t->jchunk / GI_NT & (t->jchunk / GI_NT - 1)) != 0))
+    if (t->jchunk < 0 || t->jchunk % gi::kPairChunk != 0 ||
+        (t->jchunk > 0 && (t->jchunk / gi::kPairChunk & (t->jchunk / gi::kPairChunk - 1)) != 0))
         return fail(GI_ERR_INVALID_ARG,
-                    "jchunk must be 0 or %d times a power of two", GI_NT);
+                    "jchunk must be 0 or %d times a power of two", gi::kPairChunk);
     c->forced = true;
     c->forced_tuning = *t;
     return GI_OK;
@@ -394,7 +395,7 @@ static void tuning_for(const gi_ctx *c, int n, int *ipt, int *jchunk)
         *ipt = c->forced_tuning.i_per_thread;
         int jc = c->forced_tuning.jchunk;
         if (jc <= 0) jc = ((std::max(n, 1) + GI_NT - 1) / GI_NT) * GI_NT;
-        *jchunk = jc;
+        *jchunk = std::max(jc, GI_NT);  // the one-sided kernel's chunks are whole tiles
         return;
     }
     const int b = bucket_of(std::max(n, 1));
@@ -442,10 +443,57 @@ static void chunking(int n, int jchunk, int *lg, int *tiles, int *nsplit)
     *nsplit = r;
 }
 
+// ---- GI_ACCUM_PAIRED decomposition (gi_force_pair.cu): i-blocks of
+// kPairRows bodies; block a covers the j-chunks from its own first body to
+// the end of the run in work items of 2^pcl chunks.
+
+// Work items of a run of n bodies with 2^pcl chunks per item.
+static long long pair_items(int n, int pcl)
+{
+    const long long C = (n + gi::kPairChunk - 1) / gi::kPairChunk;
+    const long long nb = (n + gi::kPairRows - 1) / gi::kPairRows;
+    const long long cpi = 1LL << pcl, q = gi::kPairBlockChunks / cpi;
+    const long long k0 = (C + cpi - 1) / cpi;
+    return nb * k0 - q * (nb * (nb - 1) / 2);
+}
+
+// Items per run the default decomposition aims at: 16,384 items are ~36
+// waves of the 456 resident CTAs (3 per SM), so the CTAs finish together,
+// while an item still spans 2^pcl chunks of j.
+constexpr long long kPairTargetItems = 16384;
+
+static int log2_floor(long long v)
+{
+    int l = 0;
+    while ((2LL << l) <= v) ++l;
+    return l;
+}
+
+// log2 of the j-chunks per item for a run of n bodies: a function of n and
+// the context's tuning table only, never of the rest of the batch.
+static int pair_pcl_for(const gi_ctx *c, int n)
+{
+    const int lmax = log2_floor(gi::kPairMaxCpi);
+    if (c->forced) {
+        int jc = c->forced_tuning.jchunk;
+        if (jc <= 0 || jc > gi::kPairMaxCpi * gi::kPairChunk) jc = gi::kPairMaxCpi * gi::kPairChunk;
+        return log2_floor(jc / gi::kPairChunk);
+    }
+    int l = 0;
+    while (l < lmax && pair_items(std::max(n, 1), l + 1) >= kPairTargetItems) ++l;
+    l += c->bucket_pshift[bucket_of(std::max(n, 1))];
+    return std::min(std::max(l, 0), lmax);
+}
+
 extern "C" int gi_ctx_get_tuning(gi_ctx *c, int n, gi_tuning *out)
 {
     if (!c || !out) return fail(GI_ERR_INVALID_ARG, "NULL argument");
     if (n < 0) return fail(GI_ERR_BAD_SIZE, "n = %d", n);
+    if (c->opt.accum == GI_ACC_PAIRED) {
+        out->i_per_thread = gi::kPairIpl;
+        out->jchunk = gi::kPairChunk << pair_pcl_for(c, n);
+        return GI_OK;
+    }
     tuning_for(c, n, &out->i_per_thread, &out->jchunk);
     return GI_OK;
 }
@@ -453,6 +501,7 @@ extern "C" int gi_ctx_get_tuning(gi_ctx *c, int n, gi_tuning *out)
 // ---------------------------------------------------------------- planning --
 
 struct Plan {
+    bool paired = false;  // GI_ACCUM_PAIRED tables (gi_force_pair.cu)
     std::vector<LaunchTable> tables;
     std::vector<int> ipt;
     std::vector<long long> bodies;  // bodies in each table's runs
@@ -491,9 +540,76 @@ static int check_runs(const gi_run *runs, int nruns, int nparams)
     return GI_OK;
 }
 
+// Fixed-point unit of a run's paired far-field sums: a power of two such
+// that n gm_max^2, a bound on any sum of a body's pair terms
+// (|G m_i m_j dp| / max(r, 1)^3 <= gm_max^2), stays below 2^62 units.
+static void pair_far_unit(int n, const PairDev &p, RunDev &d)
+{
+    const double g = std::max(std::fabs((double)p.gm_fe), std::fabs((double)p.gm_si));
+    const int e = log2_floor(std::max(n, 2) - 1) + 1;  // 2^e >= n
+    int E = (g > 0.0 ? std::ilogb(g * g) + 1 : 0) + e - 62;
+    E = std::min(std::max(E, -126), 126);  // 2^-E is a normal float
+    d.far_unit = std::ldexp(1.0, E);
+    d.far_inv = (float)std::ldexp(1.0, -E);
+}
+
+static int make_pair_plan(const gi_ctx *c, const gi_run *runs, int nruns,
+                          const std::vector<PairDev> &pd, Plan &plan)
+{
+    plan.paired = true;
+    std::vector<int> order;
+    for (int r = 0; r < nruns; ++r) {
+        if (runs[r].n <= 0) continue;
+        order.push_back(r);
+        plan.max_end = std::max(plan.max_end, runs[r].offset + runs[r].n);
+    }
+    // big runs first, so that their CTAs start first
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return runs[a].n > runs[b].n; });
+    size_t k = 0;
+    while (k < order.size()) {
+        LaunchTable t;
+        std::memset(&t, 0, sizeof t);
+        t.sep_test = c->opt.sep_test;
+        t.dense_min = c->opt.dense_min > 0 ? c->opt.dense_min : 256;
+        long long items = 0, nb = 0;
+        while (k < order.size() && t.nruns < GI_MAX_RUNS) {
+            const gi_run &q = runs[order[k]];
+            RunDev &d = t.runs[t.nruns++];
+            d.offset = q.offset;
+            d.n = q.n;
+            d.nfe = q.nfe;
+            d.param = q.params;
+            d.ipt = gi::kPairIpl;
+            d.pcl = pair_pcl_for(c, q.n);
+            d.pnc = (q.n + gi::kPairChunk - 1) / gi::kPairChunk;
+            d.pnb = (q.n + gi::kPairRows - 1) / gi::kPairRows;
+            d.pk0 = (d.pnc + (1 << d.pcl) - 1) >> d.pcl;
+            pair_far_unit(q.n, pd[q.params], d);
+            d.item_start = (int)std::min(items, 0x7fffffffLL);
+            items += pair_items(q.n, d.pcl);
+            nb += q.n;
+            d.dt = q.dt;
+            d.dtm_fe = q.dt_over_mass_fe;
+            d.dtm_si = q.dt_over_mass_si;
+            d.damp = q.damp;
+            ++k;
+        }
+        if (items > 0x7fffffffLL) return fail(GI_ERR_BAD_SIZE, "too many work items");
+        t.nitems = (int)items;
+        for (size_t m = 0; m < pd.size(); ++m) t.params[m] = pd[m];
+        plan.tables.push_back(t);
+        plan.ipt.push_back(gi::kPairIpl);
+        plan.bodies.push_back(nb);
+        plan.ticks.push_back(0);
+    }
+    return GI_OK;
+}
+
 static int make_plan(const gi_ctx *c, const gi_run *runs, int nruns,
                      const std::vector<PairDev> &pd, Plan &plan)
 {
+    if (c->opt.accum == GI_ACC_PAIRED) return make_pair_plan(c, runs, nruns, pd, plan);
     // Group runs by i-bodies-per-thread (one kernel instance per group), big
     // runs first so their CTAs start first.
     std::vector<int> order;
@@ -676,11 +792,36 @@ static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, i
         a.queue = x->queue;
         a.delta = x->delta;
         a.fsum = x->fsum;
+        a.fsum_fx = nullptr;
         int maxn = 0;
         long long pairs = 0;
         for (int r = 0; r < tab.nruns; ++r) {
             maxn = std::max(maxn, tab.runs[r].n);
             pairs += (long long)tab.runs[r].n * tab.runs[r].n;
+        }
+        if (plan.paired) {
+            // The far-field sums start at zero; captured with the launches
+            // when the stream is capturing.
+            a.fsum_fx = reinterpret_cast<long long *>(x->fsum);
+            GI_CUDA(cudaMemsetAsync(a.fsum_fx, 0, (size_t)plan.max_end * 3 * sizeof(long long), s),
+                    "cudaMemsetAsync far-field sums");
+            if (pairs >= kOverlapMaxPairs) {
+                GI_CUDA(gi_launch_contacts(pos, vel, tab, plan.bodies[t], plan.max_end,
+                                           x->grid_work, x->delta, c->sm_count, s),
+                        "contact pass");
+                GI_CUDA(gi_launch_pair_force(a, tab, s), "paired force kernel launch");
+            } else {
+                GI_CUDA(cudaEventRecord(x->ev_fork, s), "cudaEventRecord");
+                GI_CUDA(cudaStreamWaitEvent(x->aux, x->ev_fork, 0), "cudaStreamWaitEvent");
+                GI_CUDA(gi_launch_contacts(pos, vel, tab, plan.bodies[t], plan.max_end,
+                                           x->grid_work, x->delta, c->sm_count, x->aux),
+                        "contact pass");
+                GI_CUDA(cudaEventRecord(x->ev_join, x->aux), "cudaEventRecord");
+                GI_CUDA(gi_launch_pair_force(a, tab, s), "paired force kernel launch");
+                GI_CUDA(cudaStreamWaitEvent(s, x->ev_join, 0), "cudaStreamWaitEvent");
+            }
+            GI_CUDA(gi_launch_pair_finish(epi, a, tab, maxn, c->sm_count, s), "epilogue launch");
+            continue;
         }
         const int p = plan.ipt[t];
         const int occ = c->occ[c->opt.accum][p];
@@ -875,9 +1016,11 @@ extern "C" int gi_step_pingpong(gi_ctx *c, float *pos_a, float *vel_a, float *po
 }
 
 // Autotuner: for each N bucket present in `runs` (its largest run stands for
-// it), time the force pass for every i-bodies-per-thread value and big-chunk
-// scale, on the caller's own bodies, and keep the fastest in the context's
-// table.  Synchronous; allocates a scratch force array for the timing.
+// it), time the force pass for every decomposition of the context's
+// accumulation mode (one-sided: i-bodies per thread and big-chunk scale;
+// paired: chunks per item) on the caller's own bodies, and keep the fastest
+// in the context's table.  Synchronous; allocates a scratch force array for
+// the timing.
 extern "C" int gi_autotune(gi_ctx *c, const float *pos, const float *vel, const gi_run *runs,
                            int nruns, const gi_pair_params *params, int nparams, void *stream)
 {
@@ -910,7 +1053,31 @@ extern "C" int gi_autotune(gi_ctx *c, const float *pos, const float *vel, const 
         c->forced = was_forced;
         return cuda_fail(ce, "autotune setup");
     }
-    for (int b = 0; b < 32 && st == GI_OK; ++b) {
+    const bool paired = c->opt.accum == GI_ACC_PAIRED;
+    for (int b = 0; b < 32 && st == GI_OK && paired; ++b) {
+        // paired far field: the chunks per item, 2^-2 .. 2^2 times the default
+        if (rep[b] < 0) continue;
+        const gi_run &q = runs[rep[b]];
+        float best = 1e30f;
+        int best_s = 0;
+        for (int sh = -2; sh <= 2 && st == GI_OK; ++sh) {
+            c->bucket_pshift[b] = sh;
+            st = gi_forces(c, pos, vel, force, &q, 1, params, nparams, stream);
+            if (st) break;
+            cudaEventRecord(e0, s);
+            for (int rep2 = 0; rep2 < 2 && st == GI_OK; ++rep2)
+                st = gi_forces(c, pos, vel, force, &q, 1, params, nparams, stream);
+            cudaEventRecord(e1, s);
+            if (st) break;
+            ce = cudaEventSynchronize(e1);
+            if (ce != cudaSuccess) { st = cuda_fail(ce, "autotune timing"); break; }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) { best = ms; best_s = sh; }
+        }
+        c->bucket_pshift[b] = best_s;
+    }
+    for (int b = 0; b < 32 && st == GI_OK && !paired; ++b) {
         if (rep[b] < 0) continue;
         const gi_run &q = runs[rep[b]];
         const bool big = q.n > 262144;

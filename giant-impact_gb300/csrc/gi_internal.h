@@ -18,7 +18,8 @@
 #define GI_FAR_J 1.0e16f
 #define GI_FAR_I (-1.0e16f)
 
-#define GI_ACC_KAHAN GI_ACCUM_KAHAN
+#define GI_ACC_PAIRED GI_ACCUM_PAIRED  // gi_force_pair.cu
+#define GI_ACC_KAHAN GI_ACCUM_KAHAN    // the one-sided kernel's modes
 #define GI_ACC_FP32 GI_ACCUM_FP32
 #define GI_ACC_FP64 GI_ACCUM_FP64
 
@@ -52,6 +53,13 @@ struct RunDev {
     long long part_base;  // first double of this run's partial sums
     float dt, dtm_fe, dtm_si, damp;
     int ipt;          // i-bodies per thread this run was planned for
+    // GI_ACC_PAIRED decomposition (gi_force_pair.cu)
+    int pcl;          // log2 of the j-chunks per work item
+    int pnc;          // j-chunks of the run, ceil(n / kPairChunk)
+    int pnb;          // i-blocks of the run, ceil(n / kPairRows)
+    int pk0;          // work items of i-block 0, ceil(pnc / 2^pcl)
+    float far_inv;    // 1 / far_unit: scale of a far-field sum into fixed point
+    double far_unit;  // fixed-point unit of the far-field sums (a power of two)
 };
 
 struct LaunchTable {
@@ -74,6 +82,7 @@ struct ForceArgs {
     unsigned int *queue;  // [0] next work item, [1] CTAs finished (zero between launches)
     const long long *delta;  // contact corrections, 3 per body, fixed point (gi_grid.cu)
     double *fsum;            // GI_EPI_SUM: far-field sums, 3 per body
+    long long *fsum_fx;      // GI_ACC_PAIRED: far-field sums, 3 per body, fixed point
 };
 
 // Launchers (gi_force_ipt*.cu).  Return cudaError_t of the launch.
@@ -89,6 +98,25 @@ int gi_force_occupancy(int ipt, int acc, int epi);
 // adds the contact corrections and stores or steps, one thread per body.
 cudaError_t gi_launch_finish(int epi, const ForceArgs &a, const LaunchTable &tab, int maxn,
                              int nsm, cudaStream_t s);
+
+// gi_force_pair.cu: the far field with each unordered pair evaluated once.
+// Its shape is fixed here, where the planner reads it.
+namespace gi {
+constexpr int kPairWarps = 4;                             // warps per CTA
+constexpr int kPairIpl = 8;                               // i-bodies per lane
+constexpr int kPairWarpRows = 32 * kPairIpl;              // 256 rows per warp
+constexpr int kPairRows = kPairWarps * kPairWarpRows;     // 1024: the i-block
+constexpr int kPairChunk = 32;                            // j-chunk: one body per lane
+constexpr int kPairBlockChunks = kPairRows / kPairChunk;  // 32
+constexpr int kPairMaxCpi = 32;                           // j-chunks per work item, at most
+static_assert(kPairMaxCpi <= kPairBlockChunks && kPairBlockChunks % kPairMaxCpi == 0,
+              "chunks per item must divide the chunks of an i-block");
+}  // namespace gi
+// Far-field sums of every body of the table's runs into a.fsum_fx (which
+// must be zero on entry); then the epilogue, as gi_launch_finish.
+cudaError_t gi_launch_pair_force(const ForceArgs &a, const LaunchTable &tab, cudaStream_t s);
+cudaError_t gi_launch_pair_finish(int epi, const ForceArgs &a, const LaunchTable &tab, int maxn,
+                                  int nsm, cudaStream_t s);
 
 // gi_grid.cu: contact corrections of every body of the table's runs into
 // delta (3 x int64 per body) through a hashed cell grid.  Its scratch layout

@@ -18,7 +18,7 @@ HEADER = os.path.join(ROOT, "include", "gi_api.h")
 
 GI_OK = 0
 GI_SEP_REF_INT, GI_SEP_SIGN = 0, 1
-GI_ACCUM_KAHAN, GI_ACCUM_FP32, GI_ACCUM_FP64 = 0, 1, 2
+GI_ACCUM_PAIRED, GI_ACCUM_FP32, GI_ACCUM_FP64, GI_ACCUM_KAHAN = 0, 1, 2, 3
 STATUS = {0: "GI_OK", 1: "GI_ERR_INVALID_ARG", 2: "GI_ERR_BAD_SIZE", 3: "GI_ERR_ALIGNMENT",
           4: "GI_ERR_CUDA", 5: "GI_ERR_TIMEOUT", 6: "GI_ERR_NO_DEVICE", 7: "GI_ERR_OUT_OF_MEMORY",
           8: "GI_ERR_PARAMS", 9: "GI_ERR_IO", 10: "GI_ERR_FORMAT", 11: "GI_ERR_CAPACITY"}
@@ -397,7 +397,7 @@ class Context:
     """Owns a gi_ctx (scratch, options, tuning) on one device."""
 
     def __init__(self, device: int = 0, sep_test: int = GI_SEP_REF_INT,
-                 accum: int = GI_ACCUM_KAHAN, dense_min: int = 0, cluster_tries: int = 0):
+                 accum: int = GI_ACCUM_PAIRED, dense_min: int = 0, cluster_tries: int = 0):
         h = C.c_void_p()
         check(lib().gi_ctx_create(C.byref(h), device))
         self.h = h
@@ -414,7 +414,7 @@ class Context:
         except Exception:
             pass
 
-    def set_options(self, sep_test=GI_SEP_REF_INT, accum=GI_ACCUM_KAHAN, dense_min=0,
+    def set_options(self, sep_test=GI_SEP_REF_INT, accum=GI_ACCUM_PAIRED, dense_min=0,
                     cluster_tries=0):
         o = Options(sep_test, accum, dense_min, cluster_tries)
         check(lib().gi_ctx_set_options(self.h, C.byref(o)))

@@ -26,7 +26,8 @@ INCLUDE = os.path.join(ROOT, "include")
 ORACLE = os.path.join(ROOT, "oracle")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["gi_force_ipt1.cu", "gi_force_ipt2.cu", "gi_force_ipt4.cu", "gi_force_ipt8.cu",
+CU_SOURCES = ["gi_force_pair.cu", "gi_force_ipt1.cu", "gi_force_ipt2.cu", "gi_force_ipt4.cu",
+              "gi_force_ipt8.cu",
               "gi_grid.cu", "gi_aux.cu", "gi_api.cu", "gi_noalloc.cu",
               "gi_server.cu", "gi_cluster.cu", "gi_drivers.cu", "gi_splat.cu"]
 CPP_SOURCES = ["gi_host.cpp", "gi_formats.cpp"]

@@ -148,14 +148,20 @@ typedef struct gi_run {
 #define GI_SEP_REF_INT 0   /* reference: int inout = dp.dv; KR if inout > 0 */
 #define GI_SEP_SIGN 1      /* KR if dp.dv > 0                               */
 
-/* Per-body force accumulation. */
-#define GI_ACCUM_KAHAN 0   /* FP32 per j-tile, Kahan-compensated across tiles */
-#define GI_ACCUM_FP32 1    /* FP32 per j-tile, plain FP32 across tiles        */
-#define GI_ACCUM_FP64 2    /* FP32 per j-tile, FP64 across tiles              */
+/* Far-field evaluation and per-body force accumulation. */
+#define GI_ACCUM_PAIRED 0  /* each unordered pair once, applied to both bodies;
+                              FP32 per 32-body j-chunk, exact 64-bit fixed
+                              point across chunks (the default)              */
+#define GI_ACCUM_FP32 1    /* every ordered pair; FP32 per 128-body j-tile,
+                              plain FP32 across tiles                        */
+#define GI_ACCUM_FP64 2    /* every ordered pair; FP32 per j-tile, FP64
+                              across tiles                                   */
+#define GI_ACCUM_KAHAN 3   /* every ordered pair; FP32 per j-tile,
+                              Kahan-compensated across tiles                 */
 
 typedef struct gi_options {
     int sep_test;          /* GI_SEP_*, default GI_SEP_REF_INT */
-    int accum;             /* GI_ACCUM_*, default GI_ACCUM_KAHAN */
+    int accum;             /* GI_ACCUM_*, 0 = GI_ACCUM_PAIRED */
     int dense_min;         /* contact pass: cells of at least this many bodies,
                               or of a quarter of it next to such a cell, take
                               the shared-memory tiled path; 0 = 256.
@@ -167,10 +173,13 @@ typedef struct gi_options {
 } gi_options;
 
 /* Work decomposition of one run (chosen per N bucket by the autotuner or
- * set explicitly).  i_per_thread in {1, 2, 4, 8}; jchunk = 128 * 2^k bodies
- * per big j-chunk (the last chunks shrink by halves to 128 bodies), or 0 =
- * the whole run in one chunk.  The result for a run depends only on these
- * two numbers, never on what else is in the batch. */
+ * set explicitly).  For the one-sided modes: i_per_thread in {1, 2, 4, 8};
+ * jchunk = 128 * 2^k bodies per big j-chunk (the last chunks shrink by
+ * halves to 128 bodies), or 0 = the whole run in one chunk.  For
+ * GI_ACCUM_PAIRED, i-blocks are 1024 bodies (8 per thread) and a work item
+ * spans min(jchunk, 1024) bodies of j (0 = 1024); i_per_thread is not used.
+ * The result for a run depends only on these numbers and n, never on what
+ * else is in the batch. */
 typedef struct gi_tuning {
     int i_per_thread;
     int jchunk;
@@ -197,8 +206,9 @@ int gi_device_info(int device, int *sm_count, int *cc_major, int *cc_minor,
 
 /* Replaces getForcesCollisionSingleGPU<<<N/256, 256>>>(Pos, Vel, Force, c)
  * (Code/ImpactCode/impactAddTime.cu:245-377, launched at :400).  Any n >= 0
- * (the reference needs n % 256 == 0).  Reference separation test, Kahan
- * accumulation.  Uses library-owned scratch on the current device. */
+ * (the reference needs n % 256 == 0).  Reference separation test, the
+ * default (paired) accumulation.  Uses library-owned scratch on the current
+ * device. */
 int gi_forces_collision(const float *pos, const float *vel, float *force,
                         const gi_force_collision_consts *c, int n, void *stream);
 

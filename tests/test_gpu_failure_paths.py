@@ -41,7 +41,7 @@ def test_forces_right_after_counters_overwritten(gi, orc, torch_cuda, n, pattern
     import gi_workloads as wl
     p = wl.params(gi)
     s = torch.cuda.current_stream().cuda_stream
-    ctx = gi.Context(0)
+    ctx = gi.Context(0, accum=gi.GI_ACCUM_KAHAN)  # the one-sided kernel's queue
     ctx.set_tuning(2, 1024)  # split j-chunks: tickets and partial sums in use
     pa, va, nfe_a = gi.ic_lattice(11, n, spacing=0.999, jitter=0.004, vel_sigma=1.0)
     pb, vb, nfe_b = gi.ic_lattice(12, n, spacing=1.001, jitter=0.006, vel_sigma=0.7)
@@ -56,7 +56,7 @@ def test_forces_right_after_counters_overwritten(gi, orc, torch_cuda, n, pattern
     ctx.forces(db.data_ptr(), dvb.data_ptr(), df.data_ptr(), [run_b], p, s)
     torch.cuda.synchronize()
     got = df.cpu().numpy()
-    fresh = gi.Context(0)
+    fresh = gi.Context(0, accum=gi.GI_ACCUM_KAHAN)
     fresh.set_tuning(2, 1024)
     dfr = torch.zeros_like(db)
     fresh.forces(db.data_ptr(), dvb.data_ptr(), dfr.data_ptr(), [run_b], p, s)

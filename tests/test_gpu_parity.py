@@ -339,24 +339,68 @@ def test_side_by_side_and_serial_paths_agree(gi, torch_cuda, ctx):
 
 
 @pytest.mark.parametrize("ipt,jchunk", [(1, 0), (2, 1024), (4, 2048), (4, 128), (1, 512), (8, 256)])
-def test_decompositions_agree(gi, orc, torch_cuda, ctx, ipt, jchunk):
+def test_decompositions_agree(gi, orc, torch_cuda, ipt, jchunk):
+    """The one-sided kernel's decompositions (i-bodies per thread, split
+    j-chunks) against the FP64 oracle."""
     p = config1_params(gi)
     pos, vel, nfe = gi.ic_lattice(9, 5000, vel_sigma=1.5)
     run = gi.Run(0, 5000, nfe, 0, 0, 0, 0, 0)
-    ctx.set_tuning(ipt, jchunk)
-    try:
-        f = gpu_forces(gi, torch_cuda, ctx, pos, vel, [run], p)
-    finally:
-        ctx.set_tuning(None)
+    c = gi.Context(0, accum=gi.GI_ACCUM_KAHAN)
+    c.set_tuning(ipt, jchunk)
+    f = gpu_forces(gi, torch_cuda, c, pos, vel, [run], p)
+    c.close()
     f64, _ = orc.forces_fp64(pos, vel, [(0, 5000, nfe, 0, 0, 0, 0, 0)], p)
     assert rel_l2(f[:, :3], f64) < FORCE_TOL
 
 
-@pytest.mark.parametrize("accum", [0, 1, 2])
+# Sizes around the paired kernel's 32-body chunks, 256-row warps and
+# 1024-row i-blocks, with the Fe/Si boundary inside a chunk, on a chunk
+# boundary, at 0 and at n.
+PAIRED_CASES = [(1, 1), (2, 1), (31, 7), (32, 32), (33, 0), (255, 255), (256, 100),
+                (257, 257), (1023, 511), (1024, 64), (1025, 1000), (2047, 1040),
+                (3000, 1100), (5000, 0)]
+
+
+@pytest.mark.parametrize("n,nfe", PAIRED_CASES)
+def test_paired_far_field_sizes(gi, orc, torch_cuda, ctx, n, nfe):
+    """Every unordered pair exactly once: any pair missed or counted twice
+    would move the force by a whole pair term, far above the tolerance."""
+    p = config1_params(gi)
+    pos, vel, _ = gi.ic_lattice(60 + n % 17, n, vel_sigma=1.2, nfe=nfe)
+    run = gi.Run(0, n, nfe, 0, 0, 0, 0, 0)
+    f = gpu_forces(gi, torch_cuda, ctx, pos, vel, [run], p)
+    f64, absf = orc.forces_fp64(pos, vel, [(0, n, nfe, 0, 0, 0, 0, 0)], p)
+    if n == 1:
+        assert np.all(f[:, :3] == 0)
+    else:
+        assert rel_l2(f[:, :3], f64) < FORCE_TOL
+        assert np.all(np.abs(f[:, :3] - f64).max(1) <= 1e-5 * absf + 1e-30)
+
+
+@pytest.mark.parametrize("jchunk", [32, 64, 128, 512, 1024, 0])
+def test_paired_chunks_per_item(gi, orc, torch_cuda, jchunk):
+    """Forced chunks per work item (1 to 32 j-chunks): each stays within
+    tolerance, and repeated calls are bit-identical."""
+    p = config1_params(gi)
+    n, nfe = 4500, 1337
+    pos, vel, _ = gi.ic_lattice(77, n, vel_sigma=1.5, nfe=nfe)
+    run = gi.Run(0, n, nfe, 0, 0, 0, 0, 0)
+    c = gi.Context(0)
+    c.set_tuning(1, jchunk)
+    assert c.get_tuning(n) == (8, min(jchunk or 1024, 1024))
+    f = gpu_forces(gi, torch_cuda, c, pos, vel, [run], p)
+    g = gpu_forces(gi, torch_cuda, c, pos, vel, [run], p)
+    c.close()
+    assert np.array_equal(f[:, :3], g[:, :3])
+    f64, _ = orc.forces_fp64(pos, vel, [(0, n, nfe, 0, 0, 0, 0, 0)], p)
+    assert rel_l2(f[:, :3], f64) < FORCE_TOL
+
+
+@pytest.mark.parametrize("accum", ["PAIRED", "FP32", "FP64", "KAHAN"])
 def test_accumulation_modes(gi, orc, torch_cuda, accum):
     p = config1_params(gi)
     pos, vel, nfe = ball_with_velocities(gi, 20000, 4)
-    c = gi.Context(0, accum=accum)
+    c = gi.Context(0, accum=getattr(gi, "GI_ACCUM_" + accum))
     run = gi.Run(0, len(pos), nfe, 0, 0, 0, 0, 0)
     c.set_tuning(4, 0)  # one chunk: the accumulation mode alone decides the error
     f = gpu_forces(gi, torch_cuda, c, pos, vel, [run], p)
@@ -365,16 +409,17 @@ def test_accumulation_modes(gi, orc, torch_cuda, accum):
     f64, _ = orc.forces_fp64(pos, vel, [(0, len(pos), nfe, 0, 0, 0, 0, 0)], p, idx=idx)
     err = rel_l2(f[idx, :3], f64)
     print(f"accum {accum}: rel L2 {err:.3e}")
-    assert err < (2e-5 if accum == 1 else FORCE_TOL)
+    assert err < (2e-5 if accum == "FP32" else FORCE_TOL)
 
 
-def test_autotune_keeps_results_within_tolerance(gi, orc, torch_cuda):
+@pytest.mark.parametrize("accum", ["PAIRED", "KAHAN"])
+def test_autotune_keeps_results_within_tolerance(gi, orc, torch_cuda, accum):
     torch = torch_cuda
     import gi_workloads as wl
     p = wl.params(gi)
     pos, vel, nfe = ball_with_velocities(gi, 20000, 23)
     run = wl.run_desc(gi, 0, 20000, nfe)
-    c = gi.Context(0)
+    c = gi.Context(0, accum=getattr(gi, "GI_ACCUM_" + accum))
     dp, dv = dev(torch, pos), dev(torch, vel)
     c.autotune(dp.data_ptr(), dv.data_ptr(), [run], p)
     tuned = c.get_tuning(20000)
@@ -383,7 +428,7 @@ def test_autotune_keeps_results_within_tolerance(gi, orc, torch_cuda):
     idx = np.arange(0, 20000, 11)
     f64, _ = orc.forces_fp64(pos, vel, [(0, 20000, nfe, 0, 0, 0, 0, 0)], p, idx=idx)
     print("tuned", tuned)
-    assert tuned[0] in (1, 2, 4)
+    assert tuned[0] in ((8,) if accum == "PAIRED" else (1, 2, 4))
     assert rel_l2(f[idx, :3], f64) < FORCE_TOL
 
 
