@@ -7,8 +7,8 @@
 // and the clamped term that gi_grid.cu corrects for r < 1).  The reference
 // evaluates every ordered pair, each thread summing the force on its own
 // body; here each pair is evaluated once and applied to both bodies, which
-// halves the pair arithmetic on the FMA pipe, the unit that bounds the far
-// field (22 -> 15 FMA-pipe lane operations per pair).
+// cuts the pair arithmetic on the FMA pipe, the unit that bounds the far
+// field, from 22 to about 15 lane operations per pair.
 //
 // Work decomposition.  An i-block is 1024 consecutive bodies of one run, one
 // CTA of 4 warps, 8 bodies per lane held in registers (packed in pairs for
@@ -29,14 +29,19 @@
 // j = (l + s) mod 32 and adds the pair to its own 8 i-sums and to a running
 // j-sum, which then moves one lane down (one shuffle per component).  After
 // 32 steps the j-sum has visited every lane and is back on lane j, holding
-// sum_i gm_i dp r^-3 over the warp's 256 i-bodies.  Per pair of i-bodies and
-// step: 3 FADD2 (dp), FMUL2 + 2 FFMA2 (r2), 2 FMNMX, 2 MUFU.RSQ, 3 FMUL2
-// (gm_i r^-3), 3 FFMA2 (i-sums), 3 FFMA2 (j-sum).
+// sum_i dp r^-3 over the warp's 256 i-bodies.  Per pair of i-bodies and
+// step: 3 FADD2 (dp), FMUL2 + 2 FFMA2 (r2), 2 FMNMX, 2 MUFU.RSQ, 2 FMUL2
+// (r^-3), 3 FFMA2 (i-sums), 3 FFMA2 (j-sum); per step 6 FADD fold the two
+// halves of the j-sum.  14.75 FMA-pipe lane operations per pair.
 //
-// Masses: w = gm_i r^-3 (gm = sqrt(G) m).  The i-sums gather w dp over the
-// chunk and are scaled by the chunk's gm_j when folded; chunks that straddle
-// the Fe/Si boundary, and the diagonal ones, take the per-pair gm_j instead.
-// The j-sum is scaled by the lane's own gm_j and negated.
+// Masses (gm = sqrt(G) m, so G m_i m_j = gm_i gm_j).  The i-sums gather
+// dp r^-3 over a chunk and are scaled by the chunk's gm_j when folded;
+// chunks that straddle the Fe/Si boundary, and the diagonal ones, take the
+// per-pair gm_j instead.  A warp's 256 rows are of one class except in the
+// one warp per run that straddles the boundary: the others scale their
+// finished i-sums and every j-sum by their gm_i, and only the straddling
+// warp multiplies gm_i into each pair.  The j-sum is scaled by the lane's own
+// gm_j and negated.
 //
 // Accumulation and determinism.  Chunk sums are FP32 (32 terms per i-body,
 // 256 per j-body and warp); the i-sums of an item are added chunk by chunk
@@ -63,9 +68,12 @@ __device__ __forceinline__ long long pair_items_before(long long a, long long k0
 }
 
 // One warp, one chunk.  cj: the chunk's 32 staged bodies (x, y, z, gm).
-// di = (warp's first row) - (chunk's first body), relative to the run; only
-// EDGE chunks use it (mask i < j) and their per-pair gm_j.
-template <bool EDGE>
+// di = (warp's first row) - (chunk's first body), relative to the run.
+//   EDGE: a diagonal chunk (only i < j) or one that straddles the Fe/Si
+//         boundary; the i-sums take the per-pair gm_j.
+//   IMIX: the warp's rows straddle the Fe/Si boundary; w takes the per-row
+//         gm_i.  Every other warp has one i mass, applied after the sums.
+template <bool EDGE, bool IMIX>
 __device__ __forceinline__ void pair_chunk(const float4 *__restrict__ cj, const int lane,
                                            const int di, const float2 (&nx)[kPairH],
                                            const float2 (&ny)[kPairH], const float2 (&nz)[kPairH],
@@ -92,7 +100,8 @@ __device__ __forceinline__ void pair_chunk(const float4 *__restrict__ cj, const 
             r2 = __ffma2_rn(dz, dz, r2);
             const float2 ri = make_float2(rsqrt_mufu(fmaxf(r2.x, 1.0f)),
                                           rsqrt_mufu(fmaxf(r2.y, 1.0f)));
-            float2 w = __fmul2_rn(__fmul2_rn(ri, ri), __fmul2_rn(ri, gi[h]));
+            float2 w = IMIX ? __fmul2_rn(__fmul2_rn(ri, ri), __fmul2_rn(ri, gi[h]))
+                            : __fmul2_rn(__fmul2_rn(ri, ri), ri);
             float2 wi = w;
             if (EDGE) {
                 // rows 2h and 2h+1 of this lane: i = di + (2h) 32 + lane
@@ -115,6 +124,56 @@ __device__ __forceinline__ void pair_chunk(const float4 *__restrict__ cj, const 
         bx = __shfl_sync(0xffffffffu, bx, lane + 1);
         by = __shfl_sync(0xffffffffu, by, lane + 1);
         bz = __shfl_sync(0xffffffffu, bz, lane + 1);
+    }
+}
+
+// One warp over the item's chunks.  The i-sums (sx, sy, sz) gather
+// sum_chunks gm_j sum_j w dp; each chunk's j-sums go, times -gm_j and
+// scale_j, into the CTA's fixed-point j-sums in shared memory.
+template <bool IMIX>
+__device__ __forceinline__ void pair_warp(const float4 *__restrict__ sp,
+                                          unsigned long long *__restrict__ sj, const int c0,
+                                          const int nch, const int wi0, const int lane,
+                                          const int nfe, const PairDev &P, const float scale_j,
+                                          const float2 (&nx)[kPairH], const float2 (&ny)[kPairH],
+                                          const float2 (&nz)[kPairH], const float2 (&gi)[kPairH],
+                                          float2 (&sx)[kPairH], float2 (&sy)[kPairH],
+                                          float2 (&sz)[kPairH])
+{
+#pragma unroll 1
+    for (int c = 0; c < nch; ++c) {
+        const int jc0 = (c0 + c) * kPairChunk;  // relative to the run
+        if (jc0 + kPairChunk <= wi0) continue;  // before this warp's rows
+        const bool diag = jc0 < wi0 + kPairWarpRows;
+        const bool straddle = jc0 < nfe && nfe < jc0 + kPairChunk;
+        float2 ax[kPairH], ay[kPairH], az[kPairH];
+#pragma unroll
+        for (int h = 0; h < kPairH; ++h) ax[h] = ay[h] = az[h] = make_float2(0.0f, 0.0f);
+        float bx, by, bz;
+        float gc;  // the chunk's gm_j, applied at the fold (1 for EDGE chunks)
+        if (diag || straddle) {
+            pair_chunk<true, IMIX>(sp + c * kPairChunk, lane, wi0 - jc0, nx, ny, nz, gi, ax, ay,
+                                   az, bx, by, bz);
+            gc = 1.0f;
+        } else {
+            pair_chunk<false, IMIX>(sp + c * kPairChunk, lane, 0, nx, ny, nz, gi, ax, ay, az, bx,
+                                    by, bz);
+            gc = jc0 < nfe ? P.gm_fe : P.gm_si;
+        }
+        // j side: lane l holds j = jc0 + l; the force on j is -gm_j times its sum
+        const float gj = -sp[c * kPairChunk + lane].w * scale_j;
+        unsigned long long *dst = sj + (size_t)(c * kPairChunk + lane) * 3;
+        atomicAdd(dst + 0, (unsigned long long)__float2ll_rn(gj * bx));
+        atomicAdd(dst + 1, (unsigned long long)__float2ll_rn(gj * by));
+        atomicAdd(dst + 2, (unsigned long long)__float2ll_rn(gj * bz));
+        // i side: fold the chunk sum, scaled by the chunk's gm_j
+        const float2 g2 = make_float2(gc, gc);
+#pragma unroll
+        for (int h = 0; h < kPairH; ++h) {
+            sx[h] = __ffma2_rn(ax[h], g2, sx[h]);
+            sy[h] = __ffma2_rn(ay[h], g2, sy[h]);
+            sz[h] = __ffma2_rn(az[h], g2, sz[h]);
+        }
     }
 }
 
@@ -156,7 +215,8 @@ pair_force_kernel(const ForceArgs a, const __grid_constant__ LaunchTable tab)
     }
     for (int u = threadIdx.x; u < nch * kPairChunk * 3; u += blockDim.x) sj[u] = 0ull;
 
-    // ---- this lane's 8 i-bodies: rows wi0 + k 32 + lane, k = 0..7
+    // ---- this lane's 8 i-bodies: rows wi0 + k 32 + lane, k = 0..7.  Rows
+    // beyond the run sit at GI_FAR_I, where r^-3 underflows to zero.
     const int wi0 = blk * kPairRows + warp * kPairWarpRows;  // relative to the run
     float2 nx[kPairH], ny[kPairH], nz[kPairH], gi[kPairH];
 #pragma unroll
@@ -181,44 +241,18 @@ pair_force_kernel(const ForceArgs a, const __grid_constant__ LaunchTable tab)
     float2 sx[kPairH], sy[kPairH], sz[kPairH];
 #pragma unroll
     for (int h = 0; h < kPairH; ++h) sx[h] = sy[h] = sz[h] = make_float2(0.0f, 0.0f);
-    const float inv = R.far_inv;
+    // A warp whose rows are all of one class takes its gm_i out of the pair
+    // loop: it scales the j-sums and the finished i-sums instead.
+    const bool imix = wi0 < nfe && nfe < wi0 + kPairWarpRows;
+    const float gmw = imix ? 1.0f : (wi0 < nfe ? P.gm_fe : P.gm_si);
+    const float inv = R.far_inv, scale_i = inv * gmw;
     __syncthreads();
 
-#pragma unroll 1
-    for (int c = 0; c < nch; ++c) {
-        const int jc0 = (c0 + c) * kPairChunk;  // relative to the run
-        if (jc0 + kPairChunk <= wi0) continue;  // before this warp's rows
-        const bool diag = jc0 < wi0 + kPairWarpRows;
-        const bool straddle = jc0 < nfe && nfe < jc0 + kPairChunk;
-        float2 ax[kPairH], ay[kPairH], az[kPairH];
-#pragma unroll
-        for (int h = 0; h < kPairH; ++h) ax[h] = ay[h] = az[h] = make_float2(0.0f, 0.0f);
-        float bx, by, bz;
-        float gc;  // the chunk's gm_j, applied at the fold (1 for EDGE chunks)
-        if (diag || straddle) {
-            pair_chunk<true>(sp + c * kPairChunk, lane, wi0 - jc0, nx, ny, nz, gi, ax, ay, az,
-                             bx, by, bz);
-            gc = 1.0f;
-        } else {
-            pair_chunk<false>(sp + c * kPairChunk, lane, 0, nx, ny, nz, gi, ax, ay, az, bx, by,
-                              bz);
-            gc = jc0 < nfe ? P.gm_fe : P.gm_si;
-        }
-        // j side: lane l holds j = jc0 + l; force on j is -gm_j * sum
-        const float gj = sp[c * kPairChunk + lane].w;
-        unsigned long long *dst = sj + (size_t)(c * kPairChunk + lane) * 3;
-        atomicAdd(dst + 0, (unsigned long long)__float2ll_rn(-gj * bx * inv));
-        atomicAdd(dst + 1, (unsigned long long)__float2ll_rn(-gj * by * inv));
-        atomicAdd(dst + 2, (unsigned long long)__float2ll_rn(-gj * bz * inv));
-        // i side: fold the chunk sum, scaled by the chunk's gm_j
-        const float2 g2 = make_float2(gc, gc);
-#pragma unroll
-        for (int h = 0; h < kPairH; ++h) {
-            sx[h] = __ffma2_rn(ax[h], g2, sx[h]);
-            sy[h] = __ffma2_rn(ay[h], g2, sy[h]);
-            sz[h] = __ffma2_rn(az[h], g2, sz[h]);
-        }
-    }
+    if (imix)
+        pair_warp<true>(sp, sj, c0, nch, wi0, lane, nfe, P, inv, nx, ny, nz, gi, sx, sy, sz);
+    else
+        pair_warp<false>(sp, sj, c0, nch, wi0, lane, nfe, P, scale_i, nx, ny, nz, gi, sx, sy,
+                         sz);
 
     // ---- i side into the global fixed-point sums
     unsigned long long *out = reinterpret_cast<unsigned long long *>(a.fsum_fx);
@@ -231,9 +265,9 @@ pair_force_kernel(const ForceArgs a, const __grid_constant__ LaunchTable tab)
             unsigned long long *o = out + 3 * (size_t)(rbeg + i);
             const float vx = e ? sx[h].y : sx[h].x, vy = e ? sy[h].y : sy[h].x,
                         vz = e ? sz[h].y : sz[h].x;
-            atomicAdd(o + 0, (unsigned long long)__float2ll_rn(vx * inv));
-            atomicAdd(o + 1, (unsigned long long)__float2ll_rn(vy * inv));
-            atomicAdd(o + 2, (unsigned long long)__float2ll_rn(vz * inv));
+            atomicAdd(o + 0, (unsigned long long)__float2ll_rn(vx * scale_i));
+            atomicAdd(o + 1, (unsigned long long)__float2ll_rn(vy * scale_i));
+            atomicAdd(o + 2, (unsigned long long)__float2ll_rn(vz * scale_i));
         }
     }
     // ---- j side of the whole CTA
