@@ -37,6 +37,12 @@ sys.path.insert(0, PKG)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 FLOP_PER_INTERACTION = 20  # conventional N-body count: 3 sub, r2 3, rsqrt, scale 4, 3 FMA x 2
+# The far field (gi::pair_force_kernel) evaluates each unordered pair once.
+# FMA-pipe lane operations per pair: 3 FADD (dp), FMUL + 2 FFMA (r2), 2 FMUL
+# (r^-3), 3 FFMA (i-sums), 3 FFMA (j-sum), 0.75 FADD (the j-sum's fold, 6 per
+# 8 pairs) and 0.09 FFMA (the i-sums' fold, 24 per 256 pairs).  Counted as
+# FFMA-equivalent flops (2 per lane operation), the unit of the FFMA peak.
+FMA_OPS_PER_PAIR = 14.84
 N_TARGET, N_IMPACTOR = 60000, 6000
 
 
@@ -277,9 +283,9 @@ def ref_gpu_baseline(gi, orc, torch, pos, vel, nfe, p, steps=6):
 
 
 def profile_traffic():
-    """DRAM bytes per launch of the force kernel from the committed ncu
-    summary (profiles/force_kernel_impact66k.json), or None."""
-    path = os.path.join(ROOT, "profiles", "force_kernel_impact66k.json")
+    """DRAM bytes per launch of the far-field kernel from the committed ncu
+    summary (profiles/pair_force_kernel_impact66k.json), or None."""
+    path = os.path.join(ROOT, "profiles", "pair_force_kernel_impact66k.json")
     try:
         with open(path) as f:
             return json.load(f)["dram_bytes_per_launch"]
@@ -597,12 +603,13 @@ def large_n_section(gi, torch, wl, ctx, peak_sustained, a):
     inter = n * (n - 1)
     ips = inter / (ms * 1e-3)
     tflops = ips * FLOP_PER_INTERACTION / 1e12
+    fma = (inter // 2) * FMA_OPS_PER_PAIR * 2 / (ms * 1e-3) / 1e12
     ipt, jchunk = ctx.get_tuning(n)
     return {"workload": "1,048,576-body target + 104,858-body impactor (config-1 density balls, "
                         "spin 0.5, 45 deg, 1.2 v_esc), one fused step per launch",
             "n_bodies": n, "steps": a.large_steps, "ms_per_step": ms, "value": ips,
             "unit": "interactions/s", "fp32_tflops": tflops,
-            "frac_of_sustained_ffma": tflops / peak_sustained,
+            "fma_pipe_tflops": fma, "frac_of_sustained_ffma": fma / peak_sustained,
             "tuning": {"i_per_thread": ipt, "jchunk": jchunk, "autotune_s": round(tune_s, 1)}}
 
 
@@ -869,7 +876,7 @@ def study_drift(a):
 
 
 def study_precision(a):
-    """Large-N precision: force error of the three accumulation modes (and of
+    """Large-N precision: force error of the four accumulation modes (and of
     the reference's kernel) against the FP64 oracle on a seeded i-subsample
     of the 1,153,434-body impact, then energy / angular-momentum drift of
     each mode over `steps` fused steps."""
@@ -901,7 +908,8 @@ def study_precision(a):
                 "median_rel": float(np.median(rel)), "p99_rel": float(np.quantile(rel, 0.99)),
                 "max_rel": float(rel.max())}
 
-    modes = [("fp32", gi.GI_ACCUM_FP32), ("kahan", gi.GI_ACCUM_KAHAN), ("fp64", gi.GI_ACCUM_FP64)]
+    modes = [("paired", gi.GI_ACCUM_PAIRED), ("fp32", gi.GI_ACCUM_FP32),
+             ("kahan", gi.GI_ACCUM_KAHAN), ("fp64", gi.GI_ACCUM_FP64)]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     for name, mode in modes:
         ctx = gi.Context(0, accum=mode)
@@ -1062,7 +1070,9 @@ def run_ours(a):
         # rate sustained over a comparable stretch (about half a second).
         peak_sustained = min(gi.measure_ffma_peak(local) for _ in range(12))
         info = gi.device_info(local)
-        achieved = inter * FLOP_PER_INTERACTION / (ms * 1e-3) / 1e12
+        conventional = inter * FLOP_PER_INTERACTION / (ms * 1e-3) / 1e12
+        pairs = inter // 2
+        achieved = pairs * FMA_OPS_PER_PAIR * 2 / (ms * 1e-3) / 1e12
         ipt, jchunk = ctx.get_tuning(n)
         traffic = profile_traffic()
         roof = {"bound": "fp32", "achieved": achieved, "peak": peak_sustained, "unit": "TFLOP/s",
@@ -1072,11 +1082,18 @@ def run_ours(a):
                                "FFMA chains per thread) on this GPU in this run, lowest of 12 "
                                "back-to-back runs; MEASURED_PEAKS.json has no FP32 figure",
                 "nominal_peak": info["sm_count"] * 128 * 2 * 2.07e9 / 1e12,
-                "kernel": f"gi::force_kernel<{ipt},KAHAN,SUM> (far field; the contact pass runs "
-                          f"beside it on a second stream, then gi::finish_kernel adds the "
-                          f"corrections and the kick-drift), one step per gi_step_pingpong call",
-                "flop_per_interaction": FLOP_PER_INTERACTION,
-                "interactions_per_launch": inter}
+                "kernel": "gi::pair_force_kernel (far field, each unordered pair once; the "
+                          "contact pass runs beside it on a second stream, then "
+                          "gi::pair_finish_kernel adds the corrections and the kick-drift), one "
+                          "step per gi_step_pingpong call",
+                "work": "FMA-pipe lane operations of the paired far field, 2 flops each "
+                        "(FFMA-equivalent, the unit of the FFMA peak), over the whole step's "
+                        "time: frac is the FMA pipe's share of the step",
+                "fma_ops_per_pair": FMA_OPS_PER_PAIR, "pairs_per_launch": pairs,
+                "conventional_tflops": conventional,
+                "conventional_note": "20 flops per ordered interaction, the usual N-body count; "
+                                     "it can exceed the FFMA peak because each pair is "
+                                     "evaluated once for two interactions"}
         cpu = None
         if not a.no_cpu_baseline:
             cpu = cpu_baseline(orc, dp.cpu().numpy(), dv.cpu().numpy(), nfe, p, a.cpu_seconds)
@@ -1102,10 +1119,11 @@ def run_ours(a):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded, settled; bench_state/impact66k_seed2.npz)",
             "config": bench_config(n, world, a.advance),
-            "impl": {"accumulation": "kahan (FP32 tiles of 128, compensated across tiles)",
+            "impl": {"accumulation": "paired (each unordered pair once; FP32 per 32-body "
+                                     "j-chunk, 64-bit fixed point across chunks)",
                      "tuning": {"i_per_thread": ipt, "jchunk": jchunk,
                                 "autotune_s": round(t_tune, 2)}},
-            "fp32_tflops": achieved, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
+            "fp32_tflops": conventional, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,
             "ref_gpu": refgpu, "accuracy": accuracy, "collision_phase": collision,
             "hbm": hbm, "large_n": large, "sweep": sweep,
             "serve": serve, "clocks": clk, "gpu_launches": 14 * a.steps,
