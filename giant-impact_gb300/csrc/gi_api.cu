@@ -457,13 +457,6 @@ static long long pair_items(int n, int pcl)
     return nb * k0 - q * (nb * (nb - 1) / 2);
 }
 
-// Items per run the default decomposition aims at: 8,192 items are ~18
-// waves of the 456 resident CTAs (3 per SM), so the CTAs finish together,
-// while an item still spans 2^pcl chunks of j.  Measured on the settled
-// 66,000-body impact (ms per fused step, median of 20): 4 chunks per item
-// 1.240, 8 (the default there) 1.226, 16 1.223, 32 1.262.
-constexpr long long kPairTargetItems = 8192;
-
 static int log2_floor(long long v)
 {
     int l = 0;
@@ -472,7 +465,15 @@ static int log2_floor(long long v)
 }
 
 // log2 of the j-chunks per item for a run of n bodies: a function of n and
-// the context's tuning table only, never of the rest of the batch.
+// the context's tuning table only, never of the rest of the batch.  The
+// default is 8 chunks below 32,768 bodies, 16 below 131,072, 32 above.
+// Each item ends with 3 global atomics per i-body, so items much shorter
+// than that lose to the flush: measured per gi_forces call on uniform balls
+// (ms, lone run / 8 runs in one call), n = 16,384: 8 chunks 0.126 / 0.713,
+// 16: 0.113 / 0.736; 25,000: 8 0.218 / 1.497; 45,000: 16 0.624 / 4.407, 32
+// 0.598 / 4.418; 66,000: 16 1.195 / 9.218, 8 1.199 / 9.338; 100,000: 16
+// 2.618 / 20.61; 142,000: 32 5.195 / 40.82; one chunk per item 1.1-1.3x
+// slower at every size.
 static int pair_pcl_for(const gi_ctx *c, int n)
 {
     const int lmax = log2_floor(gi::kPairMaxCpi);
@@ -481,8 +482,7 @@ static int pair_pcl_for(const gi_ctx *c, int n)
         if (jc <= 0 || jc > gi::kPairMaxCpi * gi::kPairChunk) jc = gi::kPairMaxCpi * gi::kPairChunk;
         return log2_floor(jc / gi::kPairChunk);
     }
-    int l = 0;
-    while (l < lmax && pair_items(std::max(n, 1), l + 1) >= kPairTargetItems) ++l;
+    int l = 3 + (n >= 32768) + (n >= 131072);
     l += c->bucket_pshift[bucket_of(std::max(n, 1))];
     return std::min(std::max(l, 0), lmax);
 }
@@ -555,6 +555,20 @@ static void pair_far_unit(int n, const PairDev &p, RunDev &d)
     d.far_inv = (float)std::ldexp(1.0, -E);
 }
 
+// Stride of a run's item permutation: coprime with the item count, about
+// the items of one i-block, so that consecutive CTAs hold different i-blocks.
+static int pair_stride(long long items, int nblocks)
+{
+    if (items <= 1) return 1;
+    long long p = std::max(1LL, items / std::max(nblocks, 1));
+    auto gcd = [](long long a, long long b) {
+        while (b) { const long long r = a % b; a = b; b = r; }
+        return a;
+    };
+    while (gcd(p, items) != 1) ++p;
+    return (int)p;
+}
+
 static int make_pair_plan(const gi_ctx *c, const gi_run *runs, int nruns,
                           const std::vector<PairDev> &pd, Plan &plan)
 {
@@ -589,7 +603,10 @@ static int make_pair_plan(const gi_ctx *c, const gi_run *runs, int nruns,
             d.pk0 = (d.pnc + (1 << d.pcl) - 1) >> d.pcl;
             pair_far_unit(q.n, pd[q.params], d);
             d.item_start = (int)std::min(items, 0x7fffffffLL);
-            items += pair_items(q.n, d.pcl);
+            const long long ri = pair_items(q.n, d.pcl);
+            items += ri;
+            d.pitems = (int)std::min(ri, 0x7fffffffLL);
+            d.pstride = pair_stride(ri, d.pnb);
             nb += q.n;
             d.dt = q.dt;
             d.dtm_fe = q.dt_over_mass_fe;

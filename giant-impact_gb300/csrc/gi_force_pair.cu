@@ -22,7 +22,11 @@
 //     those bodies meets this warp's bodies as its j).
 // Items are numbered block-major; block a has ceil((C - 32 a) / cpi) of them
 // (C = chunks of the run; cpi divides 32, so this is k0 - a 32 / cpi and the
-// items before block a are an arithmetic series, decoded by bisection).
+// items before block a are an arithmetic series, decoded by bisection).  CTA
+// t of a run takes item (t * stride) mod items, the stride coprime with the
+// item count and about one i-block's items long: CTAs resident together then
+// hold different i-blocks, so their i-side atomics do not queue on the same
+// addresses.
 //
 // Inner loop (per warp and chunk): the chunk is staged in shared memory as
 // (x, y, z, gm).  Lane l starts with j = l; at step s it meets
@@ -189,8 +193,10 @@ pair_force_kernel(const ForceArgs a, const __grid_constant__ LaunchTable tab)
     float4 *sp = pair_smem;                                       // cpi * 32 bodies
     unsigned long long *sj = reinterpret_cast<unsigned long long *>(pair_smem + cpi * kPairChunk);
 
-    // ---- decode (i-block a, item k of the block)
-    const long long t = item - R.item_start;
+    // ---- decode (i-block a, item k of the block).  Consecutive CTAs take
+    // items a stride apart, so the CTAs running at once work on different
+    // i-blocks and their sums land on different addresses.
+    const long long t = ((long long)(item - R.item_start) * R.pstride) % R.pitems;
     const long long k0 = R.pk0, q = kPairBlockChunks >> R.pcl;
     int lo = 0, hi = R.pnb - 1;
     while (lo < hi) {

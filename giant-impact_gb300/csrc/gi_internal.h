@@ -58,6 +58,8 @@ struct RunDev {
     int pnc;          // j-chunks of the run, ceil(n / kPairChunk)
     int pnb;          // i-blocks of the run, ceil(n / kPairRows)
     int pk0;          // work items of i-block 0, ceil(pnc / 2^pcl)
+    int pitems;       // work items of the run
+    int pstride;      // CTA t of the run takes item (t * pstride) mod pitems (coprime)
     float far_inv;    // 1 / far_unit: scale of a far-field sum into fixed point
     double far_unit;  // fixed-point unit of the far-field sums (a power of two)
 };
