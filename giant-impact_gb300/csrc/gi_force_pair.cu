@@ -181,7 +181,10 @@ __device__ __forceinline__ void pair_warp(const float4 *__restrict__ sp,
     }
 }
 
-__global__ void __launch_bounds__(kPairWarps * 32, 3)
+// 152 registers (no spills): 3 CTAs per SM use 58,368 of the 65,536, and a
+// 64-thread block of the contact pass fits beside them on every SM (about
+// 1 % per fused step against 168 registers, which fill the SM).
+__global__ void __maxnreg__(152)
 pair_force_kernel(const ForceArgs a, const __grid_constant__ LaunchTable tab)
 {
     extern __shared__ float4 pair_smem[];

@@ -543,7 +543,7 @@ contact_kernel(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                unsigned int mask, long long *__restrict__ delta,
                const __grid_constant__ LaunchTable tab)
 {
-    __shared__ unsigned int hitq[8][96];  // per warp: queued hit slots (up to 31 + 64)
+    __shared__ unsigned int hitq[8][96];  // per warp (up to 8): queued hit slots (up to 31 + 64)
     const RunDev &R = tab.runs[blockIdx.y];
     const int lane = threadIdx.x & 31;
     const int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -1060,9 +1060,11 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
                                               raw);
     const int go = (int)std::min<size_t>((icap + 255) / 256, 4 * (size_t)nsm);
     gi::dense_order_kernel<<<go, 256, 0, s>>>(raw, ctr, items);
-    const dim3 gc((maxn + 7) / 8, tab.nruns);
-    gi::contact_kernel<<<gc, 256, 0, s>>>(pos, vel, spos, svel, cursor, sorted, keys, state, m - 1,
-                                          delta, tab);
+    // 64-thread blocks (2 bodies): small enough to run beside the far
+    // field's CTAs in the registers they leave free.
+    const dim3 gc((maxn + 1) / 2, tab.nruns);
+    gi::contact_kernel<<<gc, 64, 0, s>>>(pos, vel, spos, svel, cursor, sorted, keys, state, m - 1,
+                                         delta, tab);
     gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(spos, svel, cursor, sorted, state, delta, tab,
                                                      items, ctr);
     return cudaGetLastError();
