@@ -482,10 +482,11 @@ static int pair_pcl_for(const gi_ctx *c, int n)
         if (jc <= 0 || jc > gi::kPairMaxCpi * gi::kPairChunk) jc = gi::kPairMaxCpi * gi::kPairChunk;
         return log2_floor(jc / gi::kPairChunk);
     }
-    int l = 3 + (n >= 32768) + (n >= 131072);
-    l += c->bucket_pshift[bucket_of(std::max(n, 1))];
+    const int l = gi_internal_pair_default_pcl(n) + c->bucket_pshift[bucket_of(std::max(n, 1))];
     return std::min(std::max(l, 0), lmax);
 }
+
+int gi_internal_pair_default_pcl(int n) { return 3 + (n >= 32768) + (n >= 131072); }
 
 extern "C" int gi_ctx_get_tuning(gi_ctx *c, int n, gi_tuning *out)
 {
@@ -569,6 +570,21 @@ static int pair_stride(long long items, int nblocks)
     return (int)p;
 }
 
+long long gi_internal_pair_run(RunDev &d, int n, int pcl, const PairDev &p, long long item_start)
+{
+    d.ipt = gi::kPairIpl;
+    d.pcl = pcl;
+    d.pnc = (n + gi::kPairChunk - 1) / gi::kPairChunk;
+    d.pnb = (n + gi::kPairRows - 1) / gi::kPairRows;
+    d.pk0 = (d.pnc + (1 << pcl) - 1) >> pcl;
+    pair_far_unit(n, p, d);
+    d.item_start = (int)std::min(item_start, 0x7fffffffLL);
+    const long long ri = pair_items(n, pcl);
+    d.pitems = (int)std::min(ri, 0x7fffffffLL);
+    d.pstride = pair_stride(ri, d.pnb);
+    return ri;
+}
+
 static int make_pair_plan(const gi_ctx *c, const gi_run *runs, int nruns,
                           const std::vector<PairDev> &pd, Plan &plan)
 {
@@ -596,17 +612,7 @@ static int make_pair_plan(const gi_ctx *c, const gi_run *runs, int nruns,
             d.n = q.n;
             d.nfe = q.nfe;
             d.param = q.params;
-            d.ipt = gi::kPairIpl;
-            d.pcl = pair_pcl_for(c, q.n);
-            d.pnc = (q.n + gi::kPairChunk - 1) / gi::kPairChunk;
-            d.pnb = (q.n + gi::kPairRows - 1) / gi::kPairRows;
-            d.pk0 = (d.pnc + (1 << d.pcl) - 1) >> d.pcl;
-            pair_far_unit(q.n, pd[q.params], d);
-            d.item_start = (int)std::min(items, 0x7fffffffLL);
-            const long long ri = pair_items(q.n, d.pcl);
-            items += ri;
-            d.pitems = (int)std::min(ri, 0x7fffffffLL);
-            d.pstride = pair_stride(ri, d.pnb);
+            items += gi_internal_pair_run(d, q.n, pair_pcl_for(c, q.n), pd[q.params], items);
             nb += q.n;
             d.dt = q.dt;
             d.dtm_fe = q.dt_over_mass_fe;

@@ -192,6 +192,12 @@ int gi_internal_fail(int status, const char *msg);
 int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d);
 // Device scratch bytes one run of n bodies needs in `ctx` (admission estimate).
 long long gi_internal_scratch_bytes(gi_ctx *ctx, int n);
+// The paired far field's decomposition of one run of n bodies with 2^pcl
+// j-chunks per work item, its items numbered from item_start: fills the
+// run's pcl ... far_inv and item_start, returns its work items.
+long long gi_internal_pair_run(RunDev &d, int n, int pcl, const PairDev &p, long long item_start);
+// log2 of the j-chunks per item of a run of n bodies without a tuning table.
+int gi_internal_pair_default_pcl(int n);
 // Device ordinal of a context (-1 for NULL).
 int gi_internal_ctx_device(gi_ctx *ctx);
 // Attempts one union-find link of gi_find_earth_moon may make (gi_options).

@@ -1,9 +1,9 @@
 // gi_noalloc.cu -- the collision force pass for callers that cannot allocate
 // device memory.
 //
-// gi_forces_collision, the regular drop-in, takes its scratch memory (work
-// queue, split tickets, partial sums, cell grid, contact corrections) from a
-// library context that grows it with cudaMalloc on first use.  Some callers
+// gi_forces_collision, the regular drop-in, takes its scratch memory
+// (far-field sums, cell grid, contact corrections) from a library context
+// that grows it with cudaMalloc on first use.  Some callers
 // cannot let a library do that:
 //   - applications that hand out device memory only from their own budget or
 //     pool (a run admitted against a fixed HBM budget, a GPU shared under a
@@ -11,15 +11,17 @@
 //     arbitrary step or silently break the budget;
 //   - latency-sensitive step loops that must not stall: cudaMalloc and
 //     cudaFree can synchronise the whole device, holding up every stream.
-// For them, gi_forces_collision_noalloc computes the same forces with all of
-// its scratch in one statically allocated device array, g_noalloc_scratch,
-// of GI_NOALLOC_BYTES (12 MiB).  Every GPU that loads the library holds that
+// For them, gi_forces_collision_noalloc computes the same forces, bit for bit
+// (the same kernels with the same default decomposition), with all of its
+// scratch in one statically allocated device array, g_noalloc_scratch, of
+// GI_NOALLOC_BYTES (8 MiB; the largest run takes 4.3 MiB of it).  Every GPU that loads the library holds that
 // array until the process exits.  The array limits a call to
 // GI_NOALLOC_MAX_BODIES (32,768) bodies; larger calls are refused.
 //
 // Every call shares the one array and leaves its contents behind: the
-// counters that must start at zero are cleared at the start of each call (in
-// stream order), everything else is fully written before it is read.  Calls
+// far-field sums and the grid's counters, which must start at zero, are
+// cleared at the start of each call (in stream order); everything else is
+// fully written before it is read.  Calls
 // that overlap on the GPU (for example on two streams) race on the array and
 // corrupt each other's results; serialise them.
 //
@@ -37,57 +39,32 @@
 
 #include "gi_internal.h"
 
-#define GI_NOALLOC_BYTES (12u << 20)
+#define GI_NOALLOC_BYTES (8u << 20)
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GI_NOALLOC_BYTES];
 
 namespace {
 
-constexpr int kIpt = 2;    // i-bodies per thread
-constexpr int kLg = 6;     // big j-chunks of 2^6 tiles (8,192 bodies)
-constexpr int kMaxSplit = 10;  // j-chunks per i-block for n <= GI_NOALLOC_MAX_BODIES
 constexpr size_t kMaxBodies = GI_NOALLOC_MAX_BODIES;
-constexpr size_t kQueueOff = 0;      // 2 x uint32, then one ticket per i-block
-constexpr size_t kCountersBytes = 4096;
-constexpr size_t kDeltaOff = kCountersBytes;  // 3 x int64 per body
-constexpr size_t kGridOff = kDeltaOff + 3 * sizeof(long long) * kMaxBodies;
+constexpr size_t kTriple = 3 * sizeof(long long);  // one int64 triple per body
+constexpr size_t kSumOff = 0;                         // far-field sums (paired kernel)
+constexpr size_t kDeltaOff = kSumOff + kTriple * kMaxBodies;  // contact corrections
+constexpr size_t kGridOff = kDeltaOff + kTriple * kMaxBodies;  // the cell grid
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Chunks per i-block for a run of T tiles with big chunks of 2^kLg tiles
-// (the layout the force kernel decodes, see tail_tiles).
-constexpr int nsplit_for(int T)
-{
-    if ((1 << kLg) >= T) return 1;
-    int r = 0;
-    long long covered = 0;
-    while (covered < T) {
-        covered = (r + 1 <= kLg) ? (1LL << (r + 1)) - 1
-                                 : (1LL << kLg) - 1 + (long long)(r + 1 - kLg) * (1LL << kLg);
-        ++r;
-    }
-    return r;
-}
-
-// The carve of the static array for a run of n bodies: counters, contact
-// corrections, the cell grid, then the split-j partial sums (sized for the
-// largest split).  Every part grows with n, so the largest run accepted is
-// the one to check; it is checked here, at compile time, so that a change of
-// the grid's layout or of the split cannot leave maximum-size calls refused.
-constexpr int tiles_for(size_t n) { return (int)((n + GI_NT - 1) / GI_NT); }
-constexpr int iblocks_for(size_t n) { return (int)((n + GI_NT * kIpt - 1) / (GI_NT * kIpt)); }
-constexpr size_t part_off_for(size_t n)
+// The carve of the static array: far-field sums and contact corrections
+// sized for the largest run, then the cell grid of this run.  The grid grows
+// with n, so the largest run accepted is the one to check; it is checked
+// here, at compile time, so that a change of the grid's layout cannot leave
+// maximum-size calls refused.
+constexpr size_t grid_end_for(size_t n)
 {
     return kGridOff + align256(gi_grid_words((long long)n, (long long)n) * sizeof(unsigned int));
 }
-constexpr size_t kPartBytes = (size_t)kMaxSplit * 3 * sizeof(double) * kMaxBodies;
-static_assert(nsplit_for(tiles_for(kMaxBodies)) <= kMaxSplit,
-              "the largest run splits into more j-chunks than the partial sums hold");
-static_assert(part_off_for(kMaxBodies) + kPartBytes <= GI_NOALLOC_BYTES,
+static_assert(grid_end_for(kMaxBodies) <= GI_NOALLOC_BYTES,
               "the static scratch does not hold the largest run");
-static_assert(2 * sizeof(unsigned int) + iblocks_for(kMaxBodies) * sizeof(unsigned int) <=
-                  kCountersBytes,
-              "the counter block does not hold the largest run's tickets");
+static_assert(kDeltaOff % 256 == 0 && kGridOff % 256 == 0, "carve offsets must stay aligned");
 
 std::mutex g_mu;
 void *g_base[64] = {nullptr};
@@ -171,67 +148,53 @@ extern "C" int gi_forces_collision_noalloc(const float *pos, const float *vel, f
     std::memset(&tab, 0, sizeof tab);
     int st = gi_internal_collision_pairdev(cc, &tab.params[0]);
     if (st) return st;
-    const int T = (n + GI_NT - 1) / GI_NT;
     RunDev &d = tab.runs[0];
     d.offset = 0;
     d.n = n;
     d.nfe = cc->NFe < n ? cc->NFe : n;
     d.param = 0;
-    d.ipt = kIpt;
-    d.nib = (n + GI_NT * kIpt - 1) / (GI_NT * kIpt);
-    d.lg = kLg;
-    d.tiles = T;
-    d.jchunk = GI_NT << kLg;
-    d.nsplit = nsplit_for(T);
-    d.item_start = 0;
-    d.tick_base = 0;
-    d.part_base = 0;
+    // The default decomposition of gi_forces_collision's context, so both
+    // entry points give the same bits.
+    const long long items = gi_internal_pair_run(d, n, gi_internal_pair_default_pcl(n),
+                                                 tab.params[0], 0);
     tab.nruns = 1;
-    tab.nitems = d.nib * d.nsplit;
+    tab.nitems = (int)items;
     tab.sep_test = GI_SEP_REF_INT;
     tab.dense_min = 256;
 
     // Carve the static array (the largest run is checked to fit at compile
     // time; this guards the arithmetic at run time as well).
-    const size_t part_off = part_off_for((size_t)n);
-    if (d.nsplit > kMaxSplit || part_off + kPartBytes > GI_NOALLOC_BYTES ||
-        2 * sizeof(unsigned int) + (size_t)d.nib * sizeof(unsigned int) > kCountersBytes)
+    if (grid_end_for((size_t)n) > GI_NOALLOC_BYTES)
         return gi_internal_fail(GI_ERR_BAD_SIZE, "static scratch layout does not fit this run");
     void *base = nullptr;
     if ((st = scratch_base(&base))) return st;
     unsigned char *b = static_cast<unsigned char *>(base);
-    unsigned int *queue = reinterpret_cast<unsigned int *>(b + kQueueOff);
-    unsigned int *tickets = queue + 2;
+    long long *sums = reinterpret_cast<long long *>(b + kSumOff);
     long long *delta = reinterpret_cast<long long *>(b + kDeltaOff);
     unsigned int *grid = reinterpret_cast<unsigned int *>(b + kGridOff);
-    double *partials = reinterpret_cast<double *>(b + part_off);
 
     int dev = 0, nsm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return gi_internal_fail(GI_ERR_CUDA, "device query failed");
     cudaStream_t s = (cudaStream_t)stream;
-    // The queue and tickets must start at zero; the array keeps whatever the
+    // The far-field sums must start at zero; the array keeps whatever the
     // previous call left, so clear them in stream order.
-    if (cudaMemsetAsync(b + kQueueOff, 0, kCountersBytes, s) != cudaSuccess)
-        return gi_internal_fail(GI_ERR_CUDA, "clearing the static scratch counters failed");
+    if (cudaMemsetAsync(sums, 0, kTriple * (size_t)n, s) != cudaSuccess)
+        return gi_internal_fail(GI_ERR_CUDA, "clearing the static scratch sums failed");
     if (gi_launch_contacts(reinterpret_cast<const float4 *>(pos), reinterpret_cast<const float4 *>(vel),
                            tab, n, n, grid, delta, nsm, s) != cudaSuccess)
         return gi_internal_fail(GI_ERR_CUDA, "contact pass launch failed");
     ForceArgs a;
+    std::memset(&a, 0, sizeof a);
     a.pos = reinterpret_cast<const float4 *>(pos);
     a.vel = reinterpret_cast<const float4 *>(vel);
     a.force = reinterpret_cast<float4 *>(force);
-    a.pos_out = nullptr;
-    a.vel_out = nullptr;
-    a.partials = partials;
-    a.tickets = tickets;
-    a.queue = queue;
     a.delta = delta;
-    a.fsum = nullptr;  // fused epilogue (GI_EPI_FORCE)
-    int occ = gi_force_occupancy(kIpt, GI_ACC_KAHAN, GI_EPI_FORCE);
-    if (occ < 1) occ = 1;
-    if (gi_launch_force(kIpt, GI_ACC_KAHAN, GI_EPI_FORCE, a, tab, nsm * occ, s) != cudaSuccess)
+    a.fsum_fx = sums;
+    if (gi_launch_pair_force(a, tab, s) != cudaSuccess)
         return gi_internal_fail(GI_ERR_CUDA, "force kernel launch failed");
+    if (gi_launch_pair_finish(GI_EPI_FORCE, a, tab, n, nsm, s) != cudaSuccess)
+        return gi_internal_fail(GI_ERR_CUDA, "epilogue launch failed");
     return GI_OK;
 }

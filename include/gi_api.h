@@ -235,14 +235,14 @@ int gi_move_damped_separate(float *pos, float *vel, const float *force,
  * the budget), and step loops that must not stall on the device-wide
  * synchronisation cudaMalloc / cudaFree can cause.  It has no counterpart in
  * the reference, which allocates nothing beyond its three body arrays.
- * All scratch lives in one static device array of 12 MiB that every GPU
+ * All scratch lives in one static device array of 8 MiB that every GPU
  * loading the library holds until exit, so a call takes at most
  * GI_NOALLOC_MAX_BODIES bodies (larger n returns GI_ERR_BAD_SIZE).  The
  * first call on a device looks the array up (cudaGetSymbolAddress); make it
  * before any stream capture.  Calls share the array: calls that overlap on
- * the GPU (e.g. on two streams) race, so serialise them.  Forces agree with
- * gi_forces_collision within the library's 1e-5 force tolerance (the
- * decomposition, hence the summation order, differs). */
+ * the GPU (e.g. on two streams) race, so serialise them.  Forces are
+ * bit-identical to gi_forces_collision's (same kernels, same default
+ * decomposition). */
 #define GI_NOALLOC_MAX_BODIES 32768
 int gi_forces_collision_noalloc(const float *pos, const float *vel, float *force,
                                 const gi_force_collision_consts *c, int n, void *stream);
