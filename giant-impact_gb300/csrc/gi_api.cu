@@ -836,13 +836,16 @@ static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, i
                         "contact pass");
                 GI_CUDA(gi_launch_pair_force(a, tab, s), "paired force kernel launch");
             } else {
+                // The far field is launched first: it is the long kernel, and
+                // a synchronous caller would otherwise wait for the contact
+                // pass's dozen launches before it starts.
                 GI_CUDA(cudaEventRecord(x->ev_fork, s), "cudaEventRecord");
                 GI_CUDA(cudaStreamWaitEvent(x->aux, x->ev_fork, 0), "cudaStreamWaitEvent");
+                GI_CUDA(gi_launch_pair_force(a, tab, s), "paired force kernel launch");
                 GI_CUDA(gi_launch_contacts(pos, vel, tab, plan.bodies[t], plan.max_end,
                                            x->grid_work, x->delta, c->sm_count, x->aux),
                         "contact pass");
                 GI_CUDA(cudaEventRecord(x->ev_join, x->aux), "cudaEventRecord");
-                GI_CUDA(gi_launch_pair_force(a, tab, s), "paired force kernel launch");
                 GI_CUDA(cudaStreamWaitEvent(s, x->ev_join, 0), "cudaStreamWaitEvent");
             }
             GI_CUDA(gi_launch_pair_finish(epi, a, tab, maxn, c->sm_count, s), "epilogue launch");
