@@ -259,6 +259,12 @@ struct StreamScratch {
     // stream: forked after the previous step, joined before the epilogue.
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // Paired far field, side-by-side path: the far field on `far` (middle
+    // priority), the grid build and tiled contacts on `aux` (highest), the
+    // warp contact kernel on `aux_lo` (lowest), so that its blocks run in
+    // the room the far field's CTAs leave rather than in their place.
+    cudaStream_t far = nullptr, aux_lo = nullptr;
+    cudaEvent_t ev_far = nullptr, ev_lo = nullptr, ev_grid = nullptr;
 };
 
 struct gi_ctx {
@@ -319,7 +325,12 @@ static void ctx_free(gi_ctx *c)
         cudaFree(x.fsum);
         if (x.ev_fork) cudaEventDestroy(x.ev_fork);
         if (x.ev_join) cudaEventDestroy(x.ev_join);
+        if (x.ev_far) cudaEventDestroy(x.ev_far);
+        if (x.ev_lo) cudaEventDestroy(x.ev_lo);
+        if (x.ev_grid) cudaEventDestroy(x.ev_grid);
         if (x.aux) cudaStreamDestroy(x.aux);
+        if (x.far) cudaStreamDestroy(x.far);
+        if (x.aux_lo) cudaStreamDestroy(x.aux_lo);
     }
     c->scratch.clear();
     cudaFree(c->mirror_pos);
@@ -725,6 +736,13 @@ static int ensure_scratch(gi_ctx *c, const Plan &plan, cudaStream_t s, StreamScr
                 "cudaStreamCreateWithPriority");
         GI_CUDA(cudaEventCreateWithFlags(&x.ev_fork, cudaEventDisableTiming), "cudaEventCreate");
         GI_CUDA(cudaEventCreateWithFlags(&x.ev_join, cudaEventDisableTiming), "cudaEventCreate");
+        GI_CUDA(cudaStreamCreateWithPriority(&x.far, cudaStreamNonBlocking, (lo + hi) / 2),
+                "cudaStreamCreateWithPriority");
+        GI_CUDA(cudaStreamCreateWithPriority(&x.aux_lo, cudaStreamNonBlocking, lo),
+                "cudaStreamCreateWithPriority");
+        GI_CUDA(cudaEventCreateWithFlags(&x.ev_far, cudaEventDisableTiming), "cudaEventCreate");
+        GI_CUDA(cudaEventCreateWithFlags(&x.ev_lo, cudaEventDisableTiming), "cudaEventCreate");
+        GI_CUDA(cudaEventCreateWithFlags(&x.ev_grid, cudaEventDisableTiming), "cudaEventCreate");
     }
     if (grow_t || !x.counters) {
         cudaFree(x.counters);
@@ -840,13 +858,19 @@ static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, i
                 // a synchronous caller would otherwise wait for the contact
                 // pass's dozen launches before it starts.
                 GI_CUDA(cudaEventRecord(x->ev_fork, s), "cudaEventRecord");
+                GI_CUDA(cudaStreamWaitEvent(x->far, x->ev_fork, 0), "cudaStreamWaitEvent");
                 GI_CUDA(cudaStreamWaitEvent(x->aux, x->ev_fork, 0), "cudaStreamWaitEvent");
-                GI_CUDA(gi_launch_pair_force(a, tab, s), "paired force kernel launch");
+                GI_CUDA(gi_launch_pair_force(a, tab, x->far), "paired force kernel launch");
+                GI_CUDA(cudaEventRecord(x->ev_far, x->far), "cudaEventRecord");
                 GI_CUDA(gi_launch_contacts(pos, vel, tab, plan.bodies[t], plan.max_end,
-                                           x->grid_work, x->delta, c->sm_count, x->aux),
+                                           x->grid_work, x->delta, c->sm_count, x->aux,
+                                           x->aux_lo, x->ev_grid),
                         "contact pass");
                 GI_CUDA(cudaEventRecord(x->ev_join, x->aux), "cudaEventRecord");
+                GI_CUDA(cudaEventRecord(x->ev_lo, x->aux_lo), "cudaEventRecord");
+                GI_CUDA(cudaStreamWaitEvent(s, x->ev_far, 0), "cudaStreamWaitEvent");
                 GI_CUDA(cudaStreamWaitEvent(s, x->ev_join, 0), "cudaStreamWaitEvent");
+                GI_CUDA(cudaStreamWaitEvent(s, x->ev_lo, 0), "cudaStreamWaitEvent");
             }
             GI_CUDA(gi_launch_pair_finish(epi, a, tab, maxn, c->sm_count, s), "epilogue launch");
             continue;

@@ -1014,7 +1014,8 @@ cudaError_t gi_bucket_scan(unsigned int *a, unsigned int m, unsigned int *sums, 
 
 cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const LaunchTable &tab,
                                long long bodies, int max_end, unsigned int *work,
-                               long long *delta, int nsm, cudaStream_t s)
+                               long long *delta, int nsm, cudaStream_t s, cudaStream_t s_warp,
+                               cudaEvent_t ev_grid)
 {
     if (tab.nruns <= 0) return cudaSuccess;
     const unsigned int m = gi_grid_buckets(bodies);
@@ -1060,11 +1061,22 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
                                               raw);
     const int go = (int)std::min<size_t>((icap + 255) / 256, 4 * (size_t)nsm);
     gi::dense_order_kernel<<<go, 256, 0, s>>>(raw, ctr, items);
-    // 64-thread blocks (2 bodies): small enough to run beside the far
-    // field's CTAs in the registers they leave free.
+    // The two contact kernels write disjoint bodies (the warp path skips
+    // tiled buckets; the tiled path adds only into tiled bodies), so the
+    // warp path may run on a stream of its own.  64-thread blocks (2
+    // bodies): small enough to run beside the far field's CTAs in the
+    // registers they leave free.
+    cudaStream_t sw = s;
+    if (s_warp && ev_grid) {
+        e = cudaEventRecord(ev_grid, s);
+        if (e != cudaSuccess) return e;
+        e = cudaStreamWaitEvent(s_warp, ev_grid, 0);
+        if (e != cudaSuccess) return e;
+        sw = s_warp;
+    }
     const dim3 gc((maxn + 1) / 2, tab.nruns);
-    gi::contact_kernel<<<gc, 64, 0, s>>>(pos, vel, spos, svel, cursor, sorted, keys, state, m - 1,
-                                         delta, tab);
+    gi::contact_kernel<<<gc, 64, 0, sw>>>(pos, vel, spos, svel, cursor, sorted, keys, state,
+                                          m - 1, delta, tab);
     gi::contact_tile_kernel<<<16 * nsm, 128, 0, s>>>(spos, svel, cursor, sorted, state, delta, tab,
                                                      items, ctr);
     return cudaGetLastError();

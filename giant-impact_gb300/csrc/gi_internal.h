@@ -168,9 +168,13 @@ constexpr size_t gi_grid_words(long long max_end, long long bodies)
            gi::kCtrWords + 3 + 8 * gi_dense_item_capacity(bodies) +
            gi_dense_bucket_capacity(bodies);
 }
+// With s_warp and ev_grid given, the warp-per-body kernel runs on s_warp
+// after the grid is built (ev_grid is recorded on s and waited on by
+// s_warp); the caller then joins s_warp as well as s.
 cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const LaunchTable &tab,
                                long long bodies, int max_end, unsigned int *work,
-                               long long *delta, int nsm, cudaStream_t s);
+                               long long *delta, int nsm, cudaStream_t s,
+                               cudaStream_t s_warp = nullptr, cudaEvent_t ev_grid = nullptr);
 
 // gi_aux.cu
 cudaError_t gi_launch_move(float4 *pos, float4 *vel, const float4 *force,
