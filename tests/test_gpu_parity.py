@@ -307,6 +307,36 @@ def test_batch_invariance(gi, torch_cuda, ctx):
         assert np.array_equal(alone[:, :3], mixed[o:o + s, :3]), k
 
 
+def test_mixed_pair_tables_and_mass_scales(gi, orc, torch_cuda, ctx):
+    """Three runs in one call, each with its own pair table, the masses 10^3
+    apart from table to table (forces 10^6 apart; stiffness scaled with
+    m^2): each run's far field sums in a fixed-point unit of its own table.
+    Every run matches the FP64 oracle and is bit-identical to the run alone."""
+    torch = torch_cuda
+    scales = [1e-3, 1.0, 1e3]
+    ps = [gi.params_from_material(1.0, 1.0, s, 0.4 * s, 5.0 * s * s, 1.5 * s * s, 0.02, 0.01,
+                                  0.002, 0.001) for s in scales]
+    sizes, nfes = [2500, 3300, 1800], [700, 1000, 0]
+    bodies = [gi.ic_lattice(80 + k, n, vel_sigma=1.0, nfe=f) for k, (n, f) in
+              enumerate(zip(sizes, nfes))]
+    pos = np.concatenate([b[0] for b in bodies])
+    vel = np.concatenate([b[1] for b in bodies])
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(int)
+    runs = [gi.Run(int(o), n, f, k, 0, 0, 0, 0) for k, (o, n, f) in
+            enumerate(zip(offs, sizes, nfes))]
+    mixed = gpu_forces(gi, torch, ctx, pos, vel, runs, ps)
+    f64, _ = orc.forces_fp64(pos, vel, [(int(o), n, f, k, 0, 0, 0, 0) for k, (o, n, f) in
+                                        enumerate(zip(offs, sizes, nfes))], ps)
+    for k, (o, n, f) in enumerate(zip(offs, sizes, nfes)):
+        err = rel_l2(mixed[o:o + n, :3], f64[o:o + n])
+        print(f"table {k} (mass x {scales[k]:g}): rel L2 {err:.3e}, |F| ~ "
+              f"{np.abs(f64[o:o + n]).mean():.3e}")
+        assert err < FORCE_TOL
+        alone = gpu_forces(gi, torch, ctx, bodies[k][0], bodies[k][1],
+                           [gi.Run(0, n, f, 0, 0, 0, 0, 0)], ps[k])
+        assert np.array_equal(alone[:, :3], mixed[o:o + n, :3]), k
+
+
 def test_side_by_side_and_serial_paths_agree(gi, torch_cuda, ctx):
     """Tables of fewer than 2^34 pairs run the contact pass beside the far
     field and finish in a separate kernel; larger ones run it first and take
