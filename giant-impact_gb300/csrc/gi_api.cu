@@ -596,6 +596,27 @@ long long gi_internal_pair_run(RunDev &d, int n, int pcl, const PairDev &p, long
     return ri;
 }
 
+extern "C" int gi_debug_pair_plan(gi_ctx *c, int n, int pcl_in, long long out[6])
+{
+    if (!out) return fail(GI_ERR_INVALID_ARG, "out is NULL");
+    if (n <= 0) return fail(GI_ERR_BAD_SIZE, "n = %d", n);
+    if (pcl_in > log2_floor(gi::kPairMaxCpi)) return fail(GI_ERR_INVALID_ARG, "pcl = %d", pcl_in);
+    RunDev d;
+    std::memset(&d, 0, sizeof d);
+    PairDev p;
+    std::memset(&p, 0, sizeof p);
+    p.gm_fe = p.gm_si = 1.0f;
+    const int pcl = pcl_in >= 0 ? pcl_in : (c ? pair_pcl_for(c, n) : gi_internal_pair_default_pcl(n));
+    const long long items = gi_internal_pair_run(d, n, pcl, p, 0);
+    out[0] = d.pcl;
+    out[1] = d.pnc;
+    out[2] = d.pnb;
+    out[3] = items;
+    out[4] = d.pstride;
+    out[5] = d.pk0;
+    return GI_OK;
+}
+
 static int make_pair_plan(const gi_ctx *c, const gi_run *runs, int nruns,
                           const std::vector<PairDev> &pd, Plan &plan)
 {

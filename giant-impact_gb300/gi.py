@@ -216,6 +216,7 @@ _SIGS = {
                      C.c_int, C.c_int, _P], C.c_int),
     "gi_measure_ffma_peak": ([C.c_int, C.POINTER(C.c_double)], C.c_int),
     "gi_debug_fill_counters": ([_P, _P, C.c_uint], C.c_int),
+    "gi_debug_pair_plan": ([_P, C.c_int, C.c_int, C.POINTER(C.c_longlong)], C.c_int),
     "gi_server_create": ([C.c_int, C.POINTER(ServerConfig), C.POINTER(PairParams), C.c_int,
                           C.POINTER(_P)], C.c_int),
     "gi_server_destroy": ([_P], C.c_int),
@@ -322,6 +323,16 @@ def _arr(structs, cls):
     structs = list(structs)
     a = (cls * max(1, len(structs)))(*structs)
     return a, len(structs)
+
+
+def pair_plan(n: int, pcl: int = -1, ctx=None) -> dict:
+    """The paired far field's decomposition of a run of n bodies with 2^pcl
+    j-chunks per item (pcl < 0: ctx's choice, or the default one): host
+    arithmetic only, usable without a GPU."""
+    out = (C.c_longlong * 6)()
+    check(lib().gi_debug_pair_plan(ctx.h if ctx is not None else None, n, pcl, out))
+    return {"pcl": out[0], "chunks": out[1], "iblocks": out[2], "items": out[3],
+            "stride": out[4], "items_block0": out[5]}
 
 
 def params_from_material(G=1.0, diameter=1.0, mass_fe=1.0, mass_si=0.4, k_fe=5.0, k_si=1.5,

@@ -263,10 +263,13 @@ int gi_ctx_set_tuning(gi_ctx *ctx, const gi_tuning *tuning);
 int gi_ctx_get_tuning(gi_ctx *ctx, int n, gi_tuning *out);
 
 /* Autotuner: for each N bucket (floor(log2 n)) among `runs`, times the
- * force pass for i_per_thread in {1, 2, 4} and five big-chunk sizes on the
- * caller's own bodies, and stores the fastest in the context (synchronous;
- * allocates a temporary force array).  Later calls decompose runs of those
- * buckets with the tuned values; results depend only on n and this table. */
+ * force pass on the caller's own bodies for every decomposition of the
+ * context's accumulation mode (GI_ACCUM_PAIRED: 2^-2 .. 2^2 times the
+ * default j-chunks per work item; the one-sided modes: i_per_thread in
+ * {1, 2, 4} and five big-chunk sizes) and stores the fastest in the context
+ * (synchronous; allocates a temporary force array).  Later calls decompose
+ * runs of those buckets with the tuned values; results depend only on n and
+ * this table. */
 int gi_autotune(gi_ctx *ctx, const float *pos, const float *vel, const gi_run *runs,
                 int nruns, const gi_pair_params *params, int nparams, void *stream);
 
@@ -350,6 +353,13 @@ int gi_measure_ffma_peak(int device, double *tflops);
  * cut short would leave them; synchronous.  The next force call must still
  * be correct, because every launch clears them first. */
 int gi_debug_fill_counters(gi_ctx *ctx, void *stream, unsigned int value);
+
+/* Test hook: the paired far field's decomposition of one run of n bodies
+ * with 2^pcl j-chunks per work item (pcl < 0: this context's choice, or the
+ * default one when ctx is NULL); host arithmetic only, no device work.
+ * out[6] = {pcl, j-chunks, i-blocks, work items, stride of the item
+ * permutation, items of i-block 0}. */
+int gi_debug_pair_plan(gi_ctx *ctx, int n, int pcl, long long out[6]);
 
 /* ------------------------------------------------------------------------ */
 /* Serving loop (continuous batching of impact runs)                        */
