@@ -254,7 +254,8 @@ struct StreamScratch {
     size_t grid_work_cap = 0;           // words
     long long *delta = nullptr;         // contact corrections, 3 per body
     size_t delta_cap = 0;               // bodies
-    double *fsum = nullptr;             // far-field sums of GI_EPI_SUM launches, 3 per body
+    double *fsum = nullptr;  // far-field sums, 3 per body: FP64 (one-sided GI_EPI_SUM launches)
+                             // or int64 fixed point (paired far field)
     // The contact pass runs on `aux`, beside the far field on the caller's
     // stream: forked after the previous step, joined before the epilogue.
     cudaStream_t aux = nullptr;

@@ -7,8 +7,9 @@
 
 #include "../../include/gi_api.h"
 
-// Threads per CTA of the force kernels; also the j-tile staged in shared
-// memory and the granularity of the Kahan fold (one fold per 128 j).
+// Threads per CTA of the one-sided force kernel (gi_force_impl.cuh); also
+// its j-tile staged in shared memory and the granularity of its Kahan fold
+// (one fold per 128 j).  The paired far field's shape is kPair* below.
 #define GI_NT 128
 // Runs and pair tables carried by value in one launch.
 #define GI_MAX_RUNS 64
