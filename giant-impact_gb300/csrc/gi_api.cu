@@ -279,7 +279,10 @@ struct gi_ctx {
     int bucket_shift[32] = {0};  // big-chunk size scale 2^shift of the default
     int bucket_pshift[32] = {0};  // GI_ACCUM_PAIRED: chunks per item scale 2^shift
     std::map<cudaStream_t, StreamScratch> scratch;
+    // gi_run_host's device copies of the caller's host state, two pairs
+    // that the steps alternate between.
     float4 *mirror_pos = nullptr, *mirror_vel = nullptr;
+    float4 *mirror2_pos = nullptr, *mirror2_vel = nullptr;
     size_t mirror_cap = 0;
     double *diag_work = nullptr;  // 16 doubles per block + 16 for the result
     int diag_blocks = 0;
@@ -336,6 +339,8 @@ static void ctx_free(gi_ctx *c)
     c->scratch.clear();
     cudaFree(c->mirror_pos);
     cudaFree(c->mirror_vel);
+    cudaFree(c->mirror2_pos);
+    cudaFree(c->mirror2_vel);
     cudaFree(c->diag_work);
     cudaFree(c->pot_buf);
 }
@@ -1206,20 +1211,50 @@ extern "C" int gi_run_host(gi_ctx *c, float *pos_host, float *vel_host, int ntot
         GI_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
         cudaFree(c->mirror_pos);
         cudaFree(c->mirror_vel);
-        c->mirror_pos = c->mirror_vel = nullptr;
+        cudaFree(c->mirror2_pos);
+        cudaFree(c->mirror2_vel);
+        c->mirror_pos = c->mirror_vel = c->mirror2_pos = c->mirror2_vel = nullptr;
         c->mirror_cap = 0;
         GI_CUDA(cudaMalloc(&c->mirror_pos, ntotal * sizeof(float4)), "cudaMalloc mirror");
         GI_CUDA(cudaMalloc(&c->mirror_vel, ntotal * sizeof(float4)), "cudaMalloc mirror");
+        GI_CUDA(cudaMalloc(&c->mirror2_pos, ntotal * sizeof(float4)), "cudaMalloc mirror");
+        GI_CUDA(cudaMalloc(&c->mirror2_vel, ntotal * sizeof(float4)), "cudaMalloc mirror");
         c->mirror_cap = ntotal;
     }
-    const size_t bytes = (size_t)ntotal * sizeof(float4);
-    GI_CUDA(cudaMemcpyAsync(c->mirror_pos, pos_host, bytes, cudaMemcpyHostToDevice, s), "H2D pos");
-    GI_CUDA(cudaMemcpyAsync(c->mirror_vel, vel_host, bytes, cudaMemcpyHostToDevice, s), "H2D vel");
-    st = gi_step(c, (float *)c->mirror_pos, (float *)c->mirror_vel, runs, nruns, params,
-                 nparams, nsteps, stream);
-    if (st) return st;
-    GI_CUDA(cudaMemcpyAsync(pos_host, c->mirror_pos, bytes, cudaMemcpyDeviceToHost, s), "D2H pos");
-    GI_CUDA(cudaMemcpyAsync(vel_host, c->mirror_vel, bytes, cudaMemcpyDeviceToHost, s), "D2H vel");
+    // Only the runs' bodies go to the device and back (contiguous runs as one
+    // copy); the rest of the host arrays is neither read nor changed.
+    std::vector<std::pair<int, int>> rng;
+    for (int r = 0; r < nruns; ++r)
+        if (runs[r].n > 0) rng.push_back({runs[r].offset, runs[r].offset + runs[r].n});
+    std::sort(rng.begin(), rng.end());
+    std::vector<std::pair<int, int>> merged;
+    for (const auto &q : rng) {
+        if (!merged.empty() && q.first == merged.back().second) merged.back().second = q.second;
+        else merged.push_back(q);
+    }
+    float4 *const hp = reinterpret_cast<float4 *>(pos_host), *const hv = reinterpret_cast<float4 *>(vel_host);
+    for (const auto &q : merged) {
+        const size_t off = (size_t)q.first, bytes = (size_t)(q.second - q.first) * sizeof(float4);
+        GI_CUDA(cudaMemcpyAsync(c->mirror_pos + off, hp + off, bytes, cudaMemcpyHostToDevice, s),
+                "H2D pos");
+        GI_CUDA(cudaMemcpyAsync(c->mirror_vel + off, hv + off, bytes, cudaMemcpyHostToDevice, s),
+                "H2D vel");
+    }
+    // Steps alternate between the two device pairs, and the result is read
+    // back from the pair that holds it (no device-to-device copy).
+    if (nsteps > 0 && !merged.empty()) {
+        st = gi_step_pingpong(c, (float *)c->mirror_pos, (float *)c->mirror_vel,
+                              (float *)c->mirror2_pos, (float *)c->mirror2_vel, runs, nruns,
+                              params, nparams, nsteps, stream);
+        if (st) return st;
+    }
+    const float4 *rp = (nsteps & 1) ? c->mirror2_pos : c->mirror_pos;
+    const float4 *rv = (nsteps & 1) ? c->mirror2_vel : c->mirror_vel;
+    for (const auto &q : merged) {
+        const size_t off = (size_t)q.first, bytes = (size_t)(q.second - q.first) * sizeof(float4);
+        GI_CUDA(cudaMemcpyAsync(hp + off, rp + off, bytes, cudaMemcpyDeviceToHost, s), "D2H pos");
+        GI_CUDA(cudaMemcpyAsync(hv + off, rv + off, bytes, cudaMemcpyDeviceToHost, s), "D2H vel");
+    }
     GI_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
     return GI_OK;
 }

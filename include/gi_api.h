@@ -336,9 +336,11 @@ int gi_potential_fp64(gi_ctx *ctx, const float *pos, const gi_run *runs,
                       int nruns, const gi_pair_params *params, int nparams,
                       double *out, void *stream);
 
-/* End-to-end call with HOST buffers: copies pos/vel (pinned or pageable) to
- * the device, runs nsteps fused steps, copies them back, synchronises.
- * What a driver does between two records (impactAddTime.cu:396-431). */
+/* End-to-end call with HOST buffers: copies the runs' bodies of pos/vel
+ * (pinned or pageable) to the device, runs nsteps fused steps, copies them
+ * back, synchronises; host bodies outside the runs are neither read nor
+ * changed.  What a driver does between two records
+ * (impactAddTime.cu:396-431). */
 int gi_run_host(gi_ctx *ctx, float *pos_host, float *vel_host, int ntotal,
                 const gi_run *runs, int nruns, const gi_pair_params *params,
                 int nparams, int nsteps, void *stream);

@@ -543,18 +543,27 @@ def test_diag_far_from_origin_and_moving(gi, orc, torch_cuda, ctx):
     assert np.array_equal(got, again)
 
 
-def test_run_host_matches_device_path(gi, torch_cuda, ctx):
+@pytest.mark.parametrize("nsteps", [0, 1, 4])
+def test_run_host_matches_device_path(gi, torch_cuda, ctx, nsteps):
+    """Host buffers in and out, with two runs and a gap between them that no
+    run covers (left as it was): the same bits as the device path, for an
+    even and an odd number of steps."""
     torch = torch_cuda
     import gi_workloads as wl
     p = wl.params(gi)
     pos, vel, nfe = gi.ic_lattice(77, 3000, vel_sigma=1.0)
-    run = wl.run_desc(gi, 0, 3000, nfe)
-    hp, hv = pos.copy(), vel.copy()
-    ctx.run_host(hp.ctypes.data, hv.ctypes.data, 3000, [run], p, 4)
-    dp, dv = dev(torch, pos), dev(torch, vel)
-    ctx.step(dp.data_ptr(), dv.data_ptr(), [run], p, 4)
+    pos2, vel2, nfe2 = gi.ic_lattice(78, 1200, vel_sigma=1.0)
+    gap = np.full((100, 4), 7.0, np.float32)
+    P = np.concatenate([pos, gap, pos2])
+    V = np.concatenate([vel, gap, vel2])
+    runs = [wl.run_desc(gi, 0, 3000, nfe), wl.run_desc(gi, 3100, 1200, nfe2)]
+    hp, hv = P.copy(), V.copy()
+    ctx.run_host(hp.ctypes.data, hv.ctypes.data, len(P), runs, p, nsteps)
+    dp, dv = dev(torch, P), dev(torch, V)
+    ctx.step(dp.data_ptr(), dv.data_ptr(), runs, p, nsteps)
     torch.cuda.synchronize()
     assert np.array_equal(hp, host(dp)) and np.array_equal(hv, host(dv))
+    assert np.array_equal(hp[3000:3100], gap) and np.array_equal(hv[3000:3100], gap)
 
 
 def test_large_n_subsample_vs_fp64(gi, orc, torch_cuda, ctx):
