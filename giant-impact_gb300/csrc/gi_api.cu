@@ -1592,11 +1592,13 @@ int gi_internal_collision_pairdev(const gi_force_collision_consts *c, PairDev *d
 long long gi_internal_scratch_bytes(gi_ctx *c, int n)
 {
     if (n <= 0) return 0;
+    // far-field sums (3 x 8 bytes a body), contact corrections and the grid
+    const long long common = 24LL * n + 24LL * n + 4LL * (long long)gi_grid_words(n, n);
+    if (c->opt.accum == GI_ACC_PAIRED) return common;
     int ipt = 1, jc = GI_NT, lg = 0, tiles = 0, nsplit = 1;
     tuning_for(c, n, &ipt, &jc);
     chunking(n, jc, &lg, &tiles, &nsplit);
     const long long partials = nsplit > 1 ? (long long)nsplit * 3 * 8 * n : 0;
-    const long long contacts = 24LL * n + 4LL * (long long)gi_grid_words(n, n);  // delta + grid
     const long long tickets = 4LL * ((n + GI_NT - 1) / GI_NT);
-    return partials + contacts + tickets;
+    return partials + common + tickets;
 }
