@@ -307,6 +307,31 @@ def test_batch_invariance(gi, torch_cuda, ctx):
         assert np.array_equal(alone[:, :3], mixed[o:o + s, :3]), k
 
 
+def test_more_runs_than_one_launch_table(gi, orc, torch_cuda, ctx):
+    """70 runs in one call: more than a launch table holds (64), so the call
+    runs two tables one after the other, each clearing and filling the
+    far-field sums.  Every run equals the run alone, bit for bit, and the
+    batch matches the FP64 oracle."""
+    torch = torch_cuda
+    import gi_workloads as wl
+    p = wl.params(gi)
+    sizes = [300 + 37 * (k % 11) for k in range(70)]
+    bodies = [gi.ic_lattice(200 + k, n, vel_sigma=1.0) for k, n in enumerate(sizes)]
+    pos = np.concatenate([b[0] for b in bodies])
+    vel = np.concatenate([b[1] for b in bodies])
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(int)
+    runs = [wl.run_desc(gi, int(o), n, b[2]) for o, n, b in zip(offs, sizes, bodies)]
+    mixed = gpu_forces(gi, torch, ctx, pos, vel, runs, p)
+    for k in (0, 33, 64, 69):
+        o, n = int(offs[k]), sizes[k]
+        alone = gpu_forces(gi, torch, ctx, bodies[k][0], bodies[k][1],
+                           [wl.run_desc(gi, 0, n, bodies[k][2])], p)
+        assert np.array_equal(alone[:, :3], mixed[o:o + n, :3]), k
+    f64, _ = orc.forces_fp64(pos, vel, [(int(o), n, b[2], 0, 0, 0, 0, 0) for o, n, b in
+                                        zip(offs, sizes, bodies)], p)
+    assert rel_l2(mixed[:, :3], f64) < FORCE_TOL
+
+
 def test_mixed_pair_tables_and_mass_scales(gi, orc, torch_cuda, ctx):
     """Three runs in one call, each with its own pair table, the masses 10^3
     apart from table to table (forces 10^6 apart; stiffness scaled with
