@@ -131,7 +131,9 @@ def replica_value(interactions_per_step: int, steps: int, max_ms: float, world: 
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks / throttle reasons sampled every 20 ms.  start()
+    returns once the first sample is written, so that the samples cover the
+    timed region that follows (nvidia-smi takes a while to start)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -148,8 +150,12 @@ class ClockSampler:
             os.close(fd)
             self.out = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=self.out, stderr=subprocess.DEVNULL)
+            t0 = time.perf_counter()
+            while (os.path.getsize(self.path) == 0 and self.proc.poll() is None
+                   and time.perf_counter() - t0 < 5.0):
+                time.sleep(0.01)
         except Exception:
             self.proc = None
 
