@@ -839,12 +839,19 @@ constexpr int kSideBySideCtas = 8;
 
 // One force evaluation (or fused step) per table.  The contact pass and the
 // far field are independent until the epilogue, so for tables of fewer than
-// kOverlapMaxPairs pairs they run side by side: the contact pass on the
-// scratch's aux stream, forked from the caller's stream; the far field on
-// the caller's stream with kSideBySideCtas resident CTAs per SM (at that
-// size it runs as fast as at full occupancy and leaves room on every SM for
-// the contact kernels); then, joined, the epilogue, with the fused
-// epilogue's arithmetic.  Either way the results are the same bits.
+// kOverlapMaxPairs pairs they run side by side, forked from the caller's
+// stream with events and joined before the epilogue:
+//   - paired far field (the default): the far field on the scratch's
+//     middle-priority stream, the grid build and the tiled contacts on the
+//     highest-priority one, the warp contacts on the lowest (their small
+//     blocks fill the registers the far field's CTAs leave free);
+//   - one-sided modes: the contact pass on the aux stream, the far field on
+//     the caller's stream with kSideBySideCtas resident CTAs per SM (at that
+//     size it runs as fast as at full occupancy and leaves room on every SM
+//     for the contact kernels).
+// The epilogue then runs on the caller's stream with the fused epilogue's
+// arithmetic.  Larger tables run the contact pass first.  Either way the
+// results are the same bits.
 static int run_force_plan(gi_ctx *c, const StreamScratch *x, const Plan &plan, int epi,
                           const float4 *pos, const float4 *vel, float4 *force,
                           float4 *pos_out, float4 *vel_out, cudaStream_t s)
