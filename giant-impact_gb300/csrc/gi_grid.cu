@@ -247,6 +247,10 @@ constexpr float kFixM = 0x1.8p46f;  // 1.5 * 2^46
 constexpr float kFixC = 0x1.8p23f;  // 1.5 * 2^23
 constexpr float kFixMax = 0x1p45f;  // largest |term| the split takes
 constexpr unsigned int kFixFold = 256;
+// A pair term is at most 2^40 (1 + 2^-16) units (see fix_in_range).
+static_assert(0x1p40f * (1.0f + 0x1p-16f) < kFixMax, "the split must take every pair term");
+// kFixFold terms of at most 2^22 each fit the 32-bit pending sums.
+static_assert((double)kFixFold * 0x1p22 < 0x1p31, "pending sums must not wrap");
 
 struct FixSum3 {
     long long x, y, z;           // folded sums
