@@ -39,10 +39,10 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 FLOP_PER_INTERACTION = 20  # conventional N-body count: 3 sub, r2 3, rsqrt, scale 4, 3 FMA x 2
 # The far field (gi::pair_force_kernel) evaluates each unordered pair once.
 # FMA-pipe lane operations per pair: 3 FADD (dp), FMUL + 2 FFMA (r2), 2 FMUL
-# (r^-3), 3 FFMA (i-sums), 3 FFMA (j-sum), 0.75 FADD (the j-sum's fold, 6 per
-# 8 pairs) and 0.09 FFMA (the i-sums' fold, 24 per 256 pairs).  Counted as
-# FFMA-equivalent flops (2 per lane operation), the unit of the FFMA peak.
-FMA_OPS_PER_PAIR = 14.84
+# (r^-3), 3 FFMA (i-sums), 3 FFMA (j-sums) and 0.09 for the i-sums' fold
+# (48 per 512 pairs).  Counted as FFMA-equivalent flops (2 per lane
+# operation), the unit of the FFMA peak.
+FMA_OPS_PER_PAIR = 14.09
 N_TARGET, N_IMPACTOR = 60000, 6000
 
 
@@ -1125,8 +1125,8 @@ def run_ours(a):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded, settled; bench_state/impact66k_seed2.npz)",
             "config": bench_config(n, world, a.advance),
-            "impl": {"accumulation": "paired (each unordered pair once; FP32 per 32-body "
-                                     "j-chunk, 64-bit fixed point across chunks)",
+            "impl": {"accumulation": "paired (each unordered pair once; FP32 per 64-body "
+                                     "j-chunk, 64-bit fixed point across items)",
                      "tuning": {"i_per_thread": ipt, "jchunk": jchunk,
                                 "autotune_s": round(t_tune, 2)}},
             "fp32_tflops": conventional, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,

@@ -388,10 +388,9 @@ extern "C" int gi_ctx_set_tuning(gi_ctx *c, const gi_tuning *t)
     if (t->i_per_thread != 1 && t->i_per_thread != 2 && t->i_per_thread != 4 &&
         t->i_per_thread != 8)
         return fail(GI_ERR_INVALID_ARG, "i_per_thread must be 1, 2, 4 or 8");
-    if (t->jchunk < 0 || t->jchunk % gi::kPairChunk != 0 ||
-        (t->jchunk > 0 && (t->jchunk / gi::kPairChunk & (t->jchunk / gi::kPairChunk - 1)) != 0))
-        return fail(GI_ERR_INVALID_ARG,
-                    "jchunk must be 0 or %d times a power of two", gi::kPairChunk);
+    if (t->jchunk < 0 || t->jchunk % 32 != 0 ||
+        (t->jchunk > 0 && (t->jchunk / 32 & (t->jchunk / 32 - 1)) != 0))
+        return fail(GI_ERR_INVALID_ARG, "jchunk must be 0 or 32 times a power of two");
     c->forced = true;
     c->forced_tuning = *t;
     return GI_OK;
@@ -483,14 +482,15 @@ static int log2_floor(long long v)
 
 // log2 of the j-chunks per item for a run of n bodies: a function of n and
 // the context's tuning table only, never of the rest of the batch.  The
-// default is 8 chunks below 32,768 bodies, 16 below 131,072, 32 above.
-// Each item ends with 3 global atomics per i-body, so items much shorter
-// than that lose to the flush: measured per gi_forces call on uniform balls
-// (ms, lone run / 8 runs in one call), n = 16,384: 8 chunks 0.126 / 0.713,
-// 16: 0.113 / 0.736; 25,000: 8 0.218 / 1.497; 45,000: 16 0.624 / 4.407, 32
-// 0.598 / 4.418; 66,000: 16 1.195 / 9.218, 8 1.199 / 9.338; 100,000: 16
-// 2.618 / 20.61; 142,000: 32 5.195 / 40.82; one chunk per item 1.1-1.3x
-// slower at every size.
+// default spans 256 j-bodies per item below 32,768 bodies (4 chunks of 64),
+// 512 below 131,072 and 1,024 above.  Each item ends with 3 global atomics
+// per i-body, so items much shorter than that lose to the flush: measured
+// with the kernel's earlier 32-body chunks per gi_forces call on uniform
+// balls (ms, lone run / 8 runs in one call; j-bodies per item), n = 16,384:
+// 256 j 0.126 / 0.713, 512 j 0.113 / 0.736; 25,000: 256 j 0.218 / 1.497;
+// 45,000: 512 j 0.624 / 4.407, 1,024 j 0.598 / 4.418; 66,000: 512 j 1.195 /
+// 9.218, 256 j 1.199 / 9.338; 100,000: 512 j 2.618 / 20.61; 142,000: 1,024 j
+// 5.195 / 40.82; 32 j per item 1.1-1.3x slower at every size.
 static int pair_pcl_for(const gi_ctx *c, int n)
 {
     const int lmax = log2_floor(gi::kPairMaxCpi);
@@ -503,7 +503,7 @@ static int pair_pcl_for(const gi_ctx *c, int n)
     return std::min(std::max(l, 0), lmax);
 }
 
-int gi_internal_pair_default_pcl(int n) { return 3 + (n >= 32768) + (n >= 131072); }
+int gi_internal_pair_default_pcl(int n) { return 2 + (n >= 32768) + (n >= 131072); }
 
 extern "C" int gi_ctx_get_tuning(gi_ctx *c, int n, gi_tuning *out)
 {

@@ -109,9 +109,9 @@ constexpr int kPairWarps = 4;                             // warps per CTA
 constexpr int kPairIpl = 8;                               // i-bodies per lane
 constexpr int kPairWarpRows = 32 * kPairIpl;              // 256 rows per warp
 constexpr int kPairRows = kPairWarps * kPairWarpRows;     // 1024: the i-block
-constexpr int kPairChunk = 32;                            // j-chunk: one body per lane
-constexpr int kPairBlockChunks = kPairRows / kPairChunk;  // 32
-constexpr int kPairMaxCpi = 32;                           // j-chunks per work item, at most
+constexpr int kPairChunk = 64;                            // j-chunk: two bodies per lane
+constexpr int kPairBlockChunks = kPairRows / kPairChunk;  // 16
+constexpr int kPairMaxCpi = 16;                           // j-chunks per work item, at most
 static_assert(kPairMaxCpi <= kPairBlockChunks && kPairBlockChunks % kPairMaxCpi == 0,
               "chunks per item must divide the chunks of an i-block");
 }  // namespace gi

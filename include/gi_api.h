@@ -177,9 +177,9 @@ typedef struct gi_options {
  * jchunk = 128 * 2^k bodies per big j-chunk (the last chunks shrink by
  * halves to 128 bodies), or 0 = the whole run in one chunk.  For
  * GI_ACCUM_PAIRED, i-blocks are 1024 bodies (8 per thread) and a work item
- * spans min(jchunk, 1024) bodies of j (0 = 1024); i_per_thread is not used.
- * The result for a run depends only on these numbers and n, never on what
- * else is in the batch. */
+ * spans jchunk bodies of j, taken to 64 .. 1024 (0 = 1024); i_per_thread
+ * is not used.  The result for a run depends only on these numbers and n,
+ * never on what else is in the batch. */
 typedef struct gi_tuning {
     int i_per_thread;
     int jchunk;

@@ -408,12 +408,12 @@ def test_decompositions_agree(gi, orc, torch_cuda, ipt, jchunk):
     assert rel_l2(f[:, :3], f64) < FORCE_TOL
 
 
-# Sizes around the paired kernel's 32-body chunks, 256-row warps and
-# 1024-row i-blocks, with the Fe/Si boundary inside a chunk, on a chunk
-# boundary, at 0 and at n.
-PAIRED_CASES = [(1, 1), (2, 1), (31, 7), (32, 32), (33, 0), (255, 255), (256, 100),
-                (257, 257), (1023, 511), (1024, 64), (1025, 1000), (2047, 1040),
-                (3000, 1100), (5000, 0)]
+# Sizes around the paired kernel's 64-body chunks (two bodies a lane),
+# 256-row warps and 1024-row i-blocks, with the Fe/Si boundary inside a
+# chunk, on a chunk boundary, at 0 and at n.
+PAIRED_CASES = [(1, 1), (2, 1), (31, 7), (32, 32), (33, 0), (63, 40), (64, 64), (65, 33),
+                (255, 255), (256, 100), (257, 257), (1023, 511), (1024, 64), (1025, 1000),
+                (2047, 1040), (3000, 1100), (5000, 0)]
 
 
 @pytest.mark.parametrize("n,nfe", PAIRED_CASES)
@@ -434,15 +434,15 @@ def test_paired_far_field_sizes(gi, orc, torch_cuda, ctx, n, nfe):
 
 @pytest.mark.parametrize("jchunk", [32, 64, 128, 512, 1024, 0])
 def test_paired_chunks_per_item(gi, orc, torch_cuda, jchunk):
-    """Forced chunks per work item (1 to 32 j-chunks): each stays within
-    tolerance, and repeated calls are bit-identical."""
+    """Forced j-bodies per work item (1 to 16 chunks of 64): each stays
+    within tolerance, and repeated calls are bit-identical."""
     p = config1_params(gi)
     n, nfe = 4500, 1337
     pos, vel, _ = gi.ic_lattice(77, n, vel_sigma=1.5, nfe=nfe)
     run = gi.Run(0, n, nfe, 0, 0, 0, 0, 0)
     c = gi.Context(0)
     c.set_tuning(1, jchunk)
-    assert c.get_tuning(n) == (8, min(jchunk or 1024, 1024))
+    assert c.get_tuning(n) == (8, max(64, min(jchunk or 1024, 1024)))
     f = gpu_forces(gi, torch_cuda, c, pos, vel, [run], p)
     g = gpu_forces(gi, torch_cuda, c, pos, vel, [run], p)
     c.close()
