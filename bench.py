@@ -1125,8 +1125,9 @@ def run_ours(a):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded, settled; bench_state/impact66k_seed2.npz)",
             "config": bench_config(n, world, a.advance),
-            "impl": {"accumulation": "paired (each unordered pair once; FP32 per 64-body "
-                                     "j-chunk, 64-bit fixed point across items)",
+            "impl": {"accumulation": "paired (each unordered pair once; FP32 within a "
+                                     "work item of 64-body j-chunks, 64-bit fixed point "
+                                     "across items)",
                      "tuning": {"i_per_thread": ipt, "jchunk": jchunk,
                                 "autotune_s": round(t_tune, 2)}},
             "fp32_tflops": conventional, "e2e": e2e, "roofline": roof, "cpu_baseline": cpu,

@@ -150,8 +150,9 @@ typedef struct gi_run {
 
 /* Far-field evaluation and per-body force accumulation. */
 #define GI_ACCUM_PAIRED 0  /* each unordered pair once, applied to both bodies;
-                              FP32 per 32-body j-chunk, exact 64-bit fixed
-                              point across chunks (the default)              */
+                              FP32 within a work item (at most 1,024 j per
+                              i-body), exact 64-bit fixed point across items
+                              (the default)                                  */
 #define GI_ACCUM_FP32 1    /* every ordered pair; FP32 per 128-body j-tile,
                               plain FP32 across tiles                        */
 #define GI_ACCUM_FP64 2    /* every ordered pair; FP32 per j-tile, FP64

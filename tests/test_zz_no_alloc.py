@@ -74,7 +74,7 @@ def test_noalloc_refuses_more_than_its_maximum(gi, torch_cuda):
 
 @pytest.mark.parametrize("n", [3000, 1])
 def test_noalloc_small_runs_match(gi, orc, torch_cuda, n):
-    """3,000 bodies: not a multiple of the far field's 32-body j-chunk or
+    """3,000 bodies: not a multiple of the far field's 64-body j-chunk or
     1,024-body i-block, with the Fe/Si boundary inside a chunk.  n = 1 is
     the self pair alone (zero force)."""
     torch = torch_cuda
