@@ -636,10 +636,11 @@ def hbm_section(gi, torch, wl, ctx, pos, vel, nfe, p, copies=128, reps=7):
       move: gi_move = one move_kernel launch, the unfused kick-drift
             (impactAddTime.cu:379-394): 80 B/body (read pos, vel, force;
             write pos, vel).
-      diag: gi_diag_fp64, scope all = diag_pass1 + diag_pass2 (FP64 mass,
-            centre of mass, momentum, kinetic energy; angular momentum about
-            the centre of mass) + two one-thread finalisers + a 120-byte
-            read-back: 2 x 32 B/body (pos + vel read per pass)."""
+      diag: gi_diag_fp64, scope all = an 8-byte ticket clear + diag_pass1 +
+            diag_pass2 (FP64 mass, centre of mass, momentum, kinetic energy;
+            angular momentum about the centre of mass; each pass finalised by
+            its last block) + a 120-byte read-back: 2 x 32 B/body (pos + vel
+            read per pass)."""
     import numpy as np
     n = len(pos) * copies
     P = torch.from_numpy(pos).cuda().repeat(copies, 1)
@@ -675,8 +676,9 @@ def hbm_section(gi, torch, wl, ctx, pos, vel, nfe, p, copies=128, reps=7):
            "l2": "flushed before every timed call (256 MB write, outside the events)"}
     for name, ms, mm, per_body, what in (
             ("move", move_ms, move_mm, 80, "move_kernel (unfused kick-drift), one launch"),
-            ("diag", diag_ms, diag_mm, 64, "gi_diag_fp64 scope all: diag_pass1 + diag_pass2 + "
-                                           "finalisers + 120-byte read-back")):
+            ("diag", diag_ms, diag_mm, 64, "gi_diag_fp64 scope all: ticket clear + diag_pass1 + "
+                                           "diag_pass2 (each finalised by its last block) + "
+                                           "120-byte read-back")):
         gbs = per_body * n / (ms * 1e-3) / 1e9
         out[name] = {"ms": ms, "ms_min_max": mm, "algorithmic_bytes": per_body * n,
                      "bytes_per_body": per_body, "gbs": gbs, "frac_of_hbm": gbs / peak,

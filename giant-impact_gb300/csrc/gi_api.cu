@@ -284,8 +284,11 @@ struct gi_ctx {
     float4 *mirror_pos = nullptr, *mirror_vel = nullptr;
     float4 *mirror2_pos = nullptr, *mirror2_vel = nullptr;
     size_t mirror_cap = 0;
-    double *diag_work = nullptr;  // 16 doubles per block + 16 for the result
-    int diag_blocks = 0;
+    // 16 doubles per block of the larger diagnostics grid, 16 for the
+    // result, then the passes' two tickets
+    double *diag_work = nullptr;
+    double *diag_host = nullptr;  // pinned: the result's read-back
+    int diag_blocks1 = 0, diag_blocks2 = 0;
     double *pot_buf = nullptr;
     size_t pot_cap = 0;
     int occ[4][9];  // resident one-sided force CTAs per SM: [accum][i-bodies per thread]
@@ -303,8 +306,9 @@ static int ctx_init(gi_ctx *c, int device)
         return fail(GI_ERR_NO_DEVICE, "libgi is built for sm_103 only; device %d is sm_%d%d",
                     device, prop.major, prop.minor);
     c->sm_count = prop.multiProcessorCount;
-    c->diag_blocks = 16 * c->sm_count;  // shared by the two material classes
     DeviceGuard g(device);
+    c->diag_blocks1 = gi_diag_blocks(1, c->sm_count);  // shared by the two material classes
+    c->diag_blocks2 = gi_diag_blocks(2, c->sm_count);
     for (int acc : {GI_ACC_KAHAN, GI_ACC_FP32, GI_ACC_FP64})
         for (int p : {1, 2, 4, 8}) {
             const int o = std::min({gi_force_occupancy(p, acc, GI_EPI_FORCE),
@@ -342,6 +346,7 @@ static void ctx_free(gi_ctx *c)
     cudaFree(c->mirror2_pos);
     cudaFree(c->mirror2_vel);
     cudaFree(c->diag_work);
+    cudaFreeHost(c->diag_host);
     cudaFree(c->pot_buf);
 }
 
@@ -1279,24 +1284,30 @@ extern "C" int gi_diag_fp64(gi_ctx *c, const float *pos, const float *vel,
     if ((st = check_body_ptr(pos, "pos")) || (st = check_body_ptr(vel, "vel"))) return st;
     DeviceGuard g(c->device);
     cudaStream_t s = (cudaStream_t)stream;
+    const size_t nbmax = (size_t)std::max(c->diag_blocks1, c->diag_blocks2);
     if (!c->diag_work) {
-        GI_CUDA(cudaMalloc(&c->diag_work, (size_t)(c->diag_blocks + 1) * 16 * sizeof(double)),
-                "cudaMalloc diag");
+        GI_CUDA(cudaMalloc(&c->diag_work, (nbmax + 2) * 16 * sizeof(double)), "cudaMalloc diag");
     }
-    double *out_dev = c->diag_work + (size_t)c->diag_blocks * 16;
+    if (!c->diag_host) {
+        GI_CUDA(cudaMallocHost(&c->diag_host, 16 * sizeof(double)), "cudaMallocHost diag");
+    }
+    double *out_dev = c->diag_work + nbmax * 16;
+    int *ticket = (int *)(c->diag_work + (nbmax + 1) * 16);
     RunDev rd;
     std::memset(&rd, 0, sizeof rd);
     rd.offset = q.offset;
     rd.n = q.n;
     rd.nfe = q.nfe;
-    PairDev pdv;
-    std::memset(&pdv, 0, sizeof pdv);
-    GI_CUDA(gi_launch_diag((const float4 *)pos, (const float4 *)vel, label, scope, rd, pdv,
-                           params->MassFe, params->MassSi, c->diag_work, c->diag_blocks,
-                           out_dev, s),
+    GI_CUDA(gi_launch_diag((const float4 *)pos, (const float4 *)vel, label, scope, rd,
+                           params->MassFe, params->MassSi, c->diag_work, c->diag_blocks1,
+                           c->diag_blocks2, out_dev, ticket, s),
             "diag launch");
-    GI_CUDA(cudaMemcpyAsync(out, out_dev, 15 * sizeof(double), cudaMemcpyDeviceToHost, s), "D2H diag");
+    // through pinned memory: a copy into the caller's pageable buffer would
+    // be staged by the driver
+    GI_CUDA(cudaMemcpyAsync(c->diag_host, out_dev, 15 * sizeof(double), cudaMemcpyDeviceToHost, s),
+            "D2H diag");
     GI_CUDA(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    std::memcpy(out, c->diag_host, 15 * sizeof(double));
     return GI_OK;
 }
 

@@ -1,6 +1,8 @@
 // gi_aux.cu -- the memory-bound kernels around the force pass: kick-drift,
 // FP64 diagnostic reductions, the pair potential, and the FFMA throughput
 // microbenchmark that gives the force kernel its roofline denominator.
+#include <algorithm>
+
 #include "gi_internal.h"
 
 namespace gi {
@@ -34,14 +36,60 @@ move_kernel(float4 *__restrict__ pos, float4 *__restrict__ vel,
 
 // ----------------------------------------------------------------- diag --
 
-__device__ __forceinline__ bool in_scope(const unsigned char *label, int i, int scope)
+// Whether a body of label l is in the scope (1: labels 1 and 2, 2: label 1,
+// 3: label 2, 4: label 3); scope 0 takes every body and reads no labels.
+__device__ __forceinline__ bool label_in_scope(unsigned char l, int scope)
 {
-    if (label == nullptr || scope == 0) return true;
-    const unsigned char l = label[i];
     if (scope == 1) return l == 1 || l == 2;
     if (scope == 2) return l == 1;
     if (scope == 3) return l == 2;
     return l == 3;
+}
+
+// Calls body(p, u) for the in-scope bodies k, k + stride, k + 2 stride, ...
+// below k1 (run-relative; off is the run's first body), in that order.  The
+// loop is software-pipelined: the next two bodies' loads (position,
+// velocity, label) are issued before the current two bodies' arithmetic, so
+// a thread always has loads in flight and the passes stream at the HBM rate
+// rather than waiting on each load.
+template <class Body>
+__device__ __forceinline__ void stream_bodies(const float4 *__restrict__ pos,
+                                              const float4 *__restrict__ vel,
+                                              const unsigned char *__restrict__ label,
+                                              int scope, int off, int k, int k1, int stride,
+                                              Body &&body)
+{
+    const bool lab = label != nullptr && scope != 0;
+    const float4 z = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float4 p0 = z, u0 = z, p1 = z, u1 = z;
+    unsigned char l0 = 0, l1 = 0;
+    bool h0 = k < k1, h1 = k + stride < k1;
+    if (h0) {
+        p0 = pos[off + k]; u0 = vel[off + k];
+        if (lab) l0 = label[off + k];
+    }
+    if (h1) {
+        p1 = pos[off + k + stride]; u1 = vel[off + k + stride];
+        if (lab) l1 = label[off + k + stride];
+    }
+    while (h0) {
+        const int kn = k + 2 * stride;
+        const bool g0 = kn < k1, g1 = kn + stride < k1;
+        float4 q0 = z, w0 = z, q1 = z, w1 = z;
+        unsigned char m0 = 0, m1 = 0;
+        if (g0) {
+            q0 = pos[off + kn]; w0 = vel[off + kn];
+            if (lab) m0 = label[off + kn];
+        }
+        if (g1) {
+            q1 = pos[off + kn + stride]; w1 = vel[off + kn + stride];
+            if (lab) m1 = label[off + kn + stride];
+        }
+        if (!lab || label_in_scope(l0, scope)) body(p0, u0);
+        if (h1 && (!lab || label_in_scope(l1, scope))) body(p1, u1);
+        p0 = q0; u0 = w0; l0 = m0; p1 = q1; u1 = w1; l1 = m1;
+        h0 = g0; h1 = g1; k = kn;
+    }
 }
 
 // The sums of the diagnostics are kept per thread in float-float pairs on
@@ -127,11 +175,15 @@ __device__ __forceinline__ void warp_ff_sum(FF (&v)[NV])
 }
 
 // Lane 0 of each warp passes its values (FP64); the block's warps are
-// added in warp order and thread c < NV writes value c of the block.
+// added in warp order and thread c < NV writes value c of the block to
+// dst.  Then each block takes a ticket: the block that takes the last one
+// returns true, after a fence, so every block's partials are visible to it.
 template <int NV>
-__device__ __forceinline__ void block_store(const double (&v)[NV], double *dst)
+__device__ __forceinline__ bool block_store_last(const double (&v)[NV], double *dst,
+                                                 int *ticket)
 {
     __shared__ double sh[NV][8];
+    __shared__ int s_last;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0) {
 #pragma unroll
@@ -144,6 +196,12 @@ __device__ __forceinline__ void block_store(const double (&v)[NV], double *dst)
         for (int w = 0; w < nw; ++w) x += sh[threadIdx.x][w];
         dst[threadIdx.x] = x;
     }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last != 0;
 }
 
 // Both passes give each block one material class, so the class mass
@@ -162,11 +220,47 @@ __device__ __forceinline__ void class_range(int nfe, int n, int nbfe, double mfe
     m = fe ? mfe : msi;
 }
 
-// Pass 1: mass, sum m x, sum m v, kinetic energy, count (9 doubles / block).
+// The block partials summed in a fixed order, by the block that finished
+// last: thread t takes blocks t, t + 256, ... in order (read past L1), then
+// a fixed shuffle tree within each warp, then the 8 warps in order.  The
+// result is deterministic for a given grid; it is valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void ordered_sums(const double *work, int nblocks, double (&res)[NV])
+{
+    __shared__ double sh[NV][8];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    double v[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) v[c] = 0.0;
+    for (int b = t; b < nblocks; b += 256)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) v[c] += __ldcg(work + 16 * b + c);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) v[c] += __shfl_down_sync(0xffffffffu, v[c], o);
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) sh[c][warp] = v[c];
+    }
+    __syncthreads();
+    if (t == 0) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            double x = 0.0;
+            for (int w = 0; w < 8; ++w) x += sh[c][w];
+            res[c] = x;
+        }
+    }
+}
+
+// Pass 1: mass, sum m x, sum m v, kinetic energy, count (9 doubles / block);
+// its last block writes out = [mass, com3, vcom3, -, -, -, ke, p3, count].
 __global__ void __launch_bounds__(256)
 diag_pass1(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
            const unsigned char *__restrict__ label, int scope, int off, int n,
-           int nfe, int nbfe, double mfe, double msi, double *__restrict__ work)
+           int nfe, int nbfe, double mfe, double msi, double *__restrict__ work,
+           int *__restrict__ ticket, double *__restrict__ out)
 {
     int k0, k1, b, nb;
     double m;
@@ -175,29 +269,19 @@ diag_pass1(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
 #pragma unroll
     for (int c = 0; c < 7; ++c) v[c] = FF{0.0f, 0.0f};
     int cnt = 0;
-    const auto body = [&](float4 p, float4 u) {
-        ff_add(v[0], p.x);
-        ff_add(v[1], p.y);
-        ff_add(v[2], p.z);
-        ff_add(v[3], u.x);
-        ff_add(v[4], u.y);
-        ff_add(v[5], u.z);
-        ff_add_prod(v[6], u.x, u.x);
-        ff_add_prod(v[6], u.y, u.y);
-        ff_add_prod(v[6], u.z, u.z);
-        ++cnt;
-    };
-    // two bodies' loads in flight at a time; each thread still takes its
-    // bodies in grid-stride order
-    const int stride = nb * blockDim.x;
-    int k = k0 + b * blockDim.x + threadIdx.x;
-    for (; k + stride < k1; k += 2 * stride) {
-        const int i0 = off + k, i1 = i0 + stride;
-        const float4 p0 = pos[i0], u0 = vel[i0], p1 = pos[i1], u1 = vel[i1];
-        if (in_scope(label, i0, scope)) body(p0, u0);
-        if (in_scope(label, i1, scope)) body(p1, u1);
-    }
-    if (k < k1 && in_scope(label, off + k, scope)) body(pos[off + k], vel[off + k]);
+    stream_bodies(pos, vel, label, scope, off, k0 + b * blockDim.x + threadIdx.x, k1,
+                  nb * blockDim.x, [&](float4 p, float4 u) {
+                      ff_add(v[0], p.x);
+                      ff_add(v[1], p.y);
+                      ff_add(v[2], p.z);
+                      ff_add(v[3], u.x);
+                      ff_add(v[4], u.y);
+                      ff_add(v[5], u.z);
+                      ff_add_prod(v[6], u.x, u.x);
+                      ff_add_prod(v[6], u.y, u.y);
+                      ff_add_prod(v[6], u.z, u.z);
+                      ++cnt;
+                  });
     warp_ff_sum<7>(v);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
@@ -205,60 +289,30 @@ diag_pass1(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
                          m * ff_value(v[0]), m * ff_value(v[1]), m * ff_value(v[2]),
                          m * ff_value(v[3]), m * ff_value(v[4]), m * ff_value(v[5]),
                          0.5 * m * ff_value(v[6]), (double)cnt};
-    block_store<9>(d, work + 16 * blockIdx.x);
-}
-
-// Block partials summed in a fixed order (thread t takes blocks t, t + 256,
-// ..., then a tree over the threads): deterministic.  Run as one block of
-// 256 threads; the sums end in sh[c][0].
-template <int NV>
-__device__ __forceinline__ void ordered_sums(const double *__restrict__ work, int nblocks,
-                                             double (&sh)[NV][256])
-{
-    const int t = threadIdx.x;
-    double v[NV];
-#pragma unroll
-    for (int c = 0; c < NV; ++c) v[c] = 0.0;
-    for (int b = t; b < nblocks; b += 256)
-#pragma unroll
-        for (int c = 0; c < NV; ++c) v[c] += work[16 * b + c];
-#pragma unroll
-    for (int c = 0; c < NV; ++c) sh[c][t] = v[c];
-    __syncthreads();
-    for (int s = 128; s > 0; s >>= 1) {
-        if (t < s)
-#pragma unroll
-            for (int c = 0; c < NV; ++c) sh[c][t] += sh[c][t + s];
-        __syncthreads();
-    }
-}
-
-// Finalise pass 1; out = [mass, com3, vcom3, -, -, -, ke, p3, count].
-__global__ void __launch_bounds__(256) diag_fin1(const double *__restrict__ work, int nblocks,
-                                                 double *out)
-{
-    __shared__ double sh[9][256];
-    ordered_sums<9>(work, nblocks, sh);
+    if (!block_store_last<9>(d, work + 16 * blockIdx.x, ticket)) return;
+    double s[9];
+    ordered_sums<9>(work, gridDim.x, s);
     if (threadIdx.x != 0) return;
-    const double m = sh[0][0];
-    out[0] = m;
+    const double M = s[0];
+    out[0] = M;
     for (int c = 0; c < 3; ++c) {
-        out[1 + c] = m > 0.0 ? sh[1 + c][0] / m : 0.0;
-        out[4 + c] = m > 0.0 ? sh[4 + c][0] / m : 0.0;
-        out[11 + c] = sh[4 + c][0];
+        out[1 + c] = M > 0.0 ? s[1 + c] / M : 0.0;
+        out[4 + c] = M > 0.0 ? s[4 + c] / M : 0.0;
+        out[11 + c] = s[4 + c];
     }
-    out[10] = sh[7][0];
-    out[14] = sh[8][0];
+    out[10] = s[7];
+    out[14] = s[8];
 }
 
 // Pass 2: angular momentum about the com, relative to the com velocity
 // (impactBasicFunctions.h:507-652 in double): r = x - com and w = v - vcom
-// as float-float pairs, sum of r x w per class.
-__global__ void __launch_bounds__(256)
+// as float-float pairs, sum of r x w per class; its last block writes
+// out[7..9].
+__global__ void __launch_bounds__(256, 4)
 diag_pass2(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
            const unsigned char *__restrict__ label, int scope, int off, int n,
-           int nfe, int nbfe, double mfe, double msi, const double *__restrict__ out,
-           double *__restrict__ work)
+           int nfe, int nbfe, double mfe, double msi, double *__restrict__ out,
+           double *__restrict__ work, int *__restrict__ ticket)
 {
     int k0, k1, b, nb;
     double m;
@@ -273,36 +327,23 @@ diag_pass2(const float4 *__restrict__ pos, const float4 *__restrict__ vel,
     FF L[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) L[c] = FF{0.0f, 0.0f};
-    const auto body = [&](float4 p, float4 u) {
-        const FF rx = ff_sub_d(p.x, ch[0], cl[0]), ry = ff_sub_d(p.y, ch[1], cl[1]),
-                 rz = ff_sub_d(p.z, ch[2], cl[2]);
-        const FF wx = ff_sub_d(u.x, ch[3], cl[3]), wy = ff_sub_d(u.y, ch[4], cl[4]),
-                 wz = ff_sub_d(u.z, ch[5], cl[5]);
-        ff_add_cross(L[0], ry, wz, rz, wy);
-        ff_add_cross(L[1], rz, wx, rx, wz);
-        ff_add_cross(L[2], rx, wy, ry, wx);
-    };
-    const int stride = nb * blockDim.x;
-    int k = k0 + b * blockDim.x + threadIdx.x;
-    for (; k + stride < k1; k += 2 * stride) {
-        const int i0 = off + k, i1 = i0 + stride;
-        const float4 p0 = pos[i0], u0 = vel[i0], p1 = pos[i1], u1 = vel[i1];
-        if (in_scope(label, i0, scope)) body(p0, u0);
-        if (in_scope(label, i1, scope)) body(p1, u1);
-    }
-    if (k < k1 && in_scope(label, off + k, scope)) body(pos[off + k], vel[off + k]);
+    stream_bodies(pos, vel, label, scope, off, k0 + b * blockDim.x + threadIdx.x, k1,
+                  nb * blockDim.x, [&](float4 p, float4 u) {
+                      const FF rx = ff_sub_d(p.x, ch[0], cl[0]), ry = ff_sub_d(p.y, ch[1], cl[1]),
+                               rz = ff_sub_d(p.z, ch[2], cl[2]);
+                      const FF wx = ff_sub_d(u.x, ch[3], cl[3]), wy = ff_sub_d(u.y, ch[4], cl[4]),
+                               wz = ff_sub_d(u.z, ch[5], cl[5]);
+                      ff_add_cross(L[0], ry, wz, rz, wy);
+                      ff_add_cross(L[1], rz, wx, rx, wz);
+                      ff_add_cross(L[2], rx, wy, ry, wx);
+                  });
     warp_ff_sum<3>(L);
     const double d[3] = {m * ff_value(L[0]), m * ff_value(L[1]), m * ff_value(L[2])};
-    block_store<3>(d, work + 16 * blockIdx.x);
-}
-
-__global__ void __launch_bounds__(256) diag_fin2(const double *__restrict__ work, int nblocks,
-                                                 double *out)
-{
-    __shared__ double sh[3][256];
-    ordered_sums<3>(work, nblocks, sh);
+    if (!block_store_last<3>(d, work + 16 * blockIdx.x, ticket)) return;
+    double s[3];
+    ordered_sums<3>(work, gridDim.x, s);
     if (threadIdx.x != 0) return;
-    out[7] = sh[0][0]; out[8] = sh[1][0]; out[9] = sh[2][0];
+    out[7] = s[0]; out[8] = s[1]; out[9] = s[2];
 }
 
 // -------------------------------------------------------------- potential --
@@ -409,25 +450,42 @@ cudaError_t gi_launch_move(float4 *pos, float4 *vel, const float4 *force,
     return cudaGetLastError();
 }
 
+// One resident wave per pass: the grid-stride loops give every block the
+// same number of bodies, so a grid of exactly the resident blocks has no
+// partial last wave.
+int gi_diag_blocks(int pass, int sm_count)
+{
+    int per_sm = 0;
+    const cudaError_t e = pass == 1
+        ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gi::diag_pass1, 256, 0)
+        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gi::diag_pass2, 256, 0);
+    if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    return std::max(2, per_sm * sm_count);
+}
+
 cudaError_t gi_launch_diag(const float4 *pos, const float4 *vel,
                            const unsigned char *label, int scope,
-                           const RunDev &run, const PairDev &par, float mass_fe,
-                           float mass_si, double *work, int nblocks, double *out_dev,
+                           const RunDev &run, float mass_fe, float mass_si, double *work,
+                           int nblocks1, int nblocks2, double *out_dev, int *ticket,
                            cudaStream_t s)
 {
-    (void)par;
+    if (nblocks1 < 2 || nblocks2 < 2) return cudaErrorInvalidValue;
     // blocks for the Fe bodies in proportion to their number (at least one
     // when there are any), the rest for the Si bodies
-    if (nblocks < 2) return cudaErrorInvalidValue;
-    int nbfe = run.n > 0 ? (int)((long long)nblocks * run.nfe / run.n) : 0;
-    if (run.nfe > 0 && nbfe < 1) nbfe = 1;
-    if (nbfe > nblocks - 1) nbfe = nblocks - 1;
-    gi::diag_pass1<<<nblocks, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
-                                           nbfe, mass_fe, mass_si, work);
-    gi::diag_fin1<<<1, 256, 0, s>>>(work, nblocks, out_dev);
-    gi::diag_pass2<<<nblocks, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
-                                           nbfe, mass_fe, mass_si, out_dev, work);
-    gi::diag_fin2<<<1, 256, 0, s>>>(work, nblocks, out_dev);
+    const auto fe_blocks = [&](int nblocks) {
+        int nbfe = run.n > 0 ? (int)((long long)nblocks * run.nfe / run.n) : 0;
+        if (run.nfe > 0 && nbfe < 1) nbfe = 1;
+        if (nbfe > nblocks - 1) nbfe = nblocks - 1;
+        return nbfe;
+    };
+    cudaError_t e = cudaMemsetAsync(ticket, 0, 2 * sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    gi::diag_pass1<<<nblocks1, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
+                                            fe_blocks(nblocks1), mass_fe, mass_si, work, ticket,
+                                            out_dev);
+    gi::diag_pass2<<<nblocks2, 256, 0, s>>>(pos, vel, label, scope, run.offset, run.n, run.nfe,
+                                            fe_blocks(nblocks2), mass_fe, mass_si, out_dev, work,
+                                            ticket + 1);
     return cudaGetLastError();
 }
 

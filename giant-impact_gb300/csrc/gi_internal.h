@@ -180,10 +180,15 @@ cudaError_t gi_launch_contacts(const float4 *pos, const float4 *vel, const Launc
 // gi_aux.cu
 cudaError_t gi_launch_move(float4 *pos, float4 *vel, const float4 *force,
                            const LaunchTable &tab, cudaStream_t s);
+// The diagnostics' blocks for pass 1 or 2: the resident blocks of that pass
+// on sm_count SMs.
+int gi_diag_blocks(int pass, int sm_count);
+// Both passes of the FP64 diagnostics; work holds 16 doubles per block of
+// the larger grid, out_dev 15 doubles, ticket 2 ints (cleared here).
 cudaError_t gi_launch_diag(const float4 *pos, const float4 *vel,
                            const unsigned char *label, int scope,
-                           const RunDev &run, const PairDev &par, float mass_fe,
-                           float mass_si, double *work, int nblocks, double *out_dev,
+                           const RunDev &run, float mass_fe, float mass_si, double *work,
+                           int nblocks1, int nblocks2, double *out_dev, int *ticket,
                            cudaStream_t s);
 cudaError_t gi_launch_potential(const float4 *pos, const LaunchTable &tab,
                                 double *per_block, int nblocks_per_run,
